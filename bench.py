@@ -1,0 +1,347 @@
+"""Benchmark: p/sec of the plain sieve on the steady-state workload.
+
+Workload ("plain_steady"): base 745, 22 seeded odd k in [3, 1e6], n in
+[180000, 250000] kept at 5%, every prime p in [1e13, 1e13 + 1e11).  One step =
+one 1e10-wide slice of that window through the hot path (device prime sieve ->
+per-prime setup -> BSGS -> verify), so the default 10 timed steps cover the
+whole window once.  Metric p/sec = width of the p-interval sieved per second,
+the reference's definition (kernel_v0.24.6.cu:1552-1554,1783).
+
+  value  device time: summed CUDA-event time of each rs_sieve_range call, from
+         its first kernel to its last, job resident in HBM.
+  e2e    the same through the C ABI from host buffers, per step: create the job
+         from its ABCD text (H2D upload), sieve the slice, copy the factors back
+         (D2H), destroy the job; host wall clock around it.
+
+Extra keys: roofline (the BSGS kernel against this GPU's measured integer
+multiply throughput), cpu_baseline (the CPU oracle on a bounded sub-window),
+clocks (nvidia-smi sampled during the timed region), gpu_launches.
+
+--impl reference times the reference's CPU path for the same metric.  The
+reference sieve (kernel_v0.24.6.cu) has no CPU implementation, so this arm runs
+the project's scalar CPU oracle (oracle/), all host cores, a bounded
+sub-window per step.
+
+Multi-GPU (torchrun, N>1): weak scaling, rank r sieves its own slices
+(step*N + r); no data-path collective, only a barrier and a max over ranks of
+the elapsed time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "cuda-riesel-sieve_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "p/sec (b=745, 22 k, n 180k–250k)"
+UNIT = "p/sec"
+P_START = 10**13
+WINDOW = 10**11
+SLICE = 10**10
+MONTMUL_MULS = 19  # 32-bit multiply-class PTX instructions per 64-bit Montgomery product
+WORKLOAD = ("plain_steady: b=745, 22 seeded odd k in [3,1e6], n in [180000,250000] at 5% density, "
+            "all primes p in [1e13, 1e13+1e11)")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (torch.distributed when N > 1)."""
+
+    def __init__(self, world: int, local: int, backend: str):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+            self.torch = torch
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64,
+                              device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64,
+                              device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(job_args, seconds: float = 12.0) -> dict:
+    """The CPU oracle on a sub-window of the workload at 1e13, all host threads."""
+    import numpy as np
+
+    import oracle
+
+    b, s, ks, nl = job_args
+    oj = oracle.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    threads = oracle.default_threads()
+    w0 = 2 * 10**6
+    t = time.perf_counter()
+    oj.sieve(P_START, P_START + w0 - 1, threads=threads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    width = int(min(5 * 10**8, max(w0, w0 * seconds / dt)))
+    t = time.perf_counter()
+    f, npr = oj.sieve(P_START + w0, P_START + w0 + width - 1, threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": width / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"p in [1e13+{w0}, +{width}) ({npr} primes, {len(f)} factors), {dt:.1f} s"}
+
+
+def run_reference(args, rank: int) -> None:
+    """The reference arm: the CPU oracle (the reference's sieve is CUDA-only)."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle
+    import rsieve.synth as S
+
+    oracle.build()
+    b, s, ks, nl = S.plain_job(1)
+    oj = oracle.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    threads = oracle.default_threads()
+    # per-step sample sized to ~3 s of CPU work
+    w0 = 10**6
+    t = time.perf_counter()
+    oj.sieve(P_START, P_START + w0 - 1, threads=threads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    width = int(min(2 * 10**8, max(w0, w0 * 3.0 / dt)))
+    a = P_START + w0
+    for _ in range(args.warmup):
+        oj.sieve(a, a + width // 4 - 1, threads=threads)
+        a += width // 4
+    t = time.perf_counter()
+    tot_f = tot_p = 0
+    for _ in range(args.steps):
+        f, npr = oj.sieve(a, a + width - 1, threads=threads)
+        tot_f += len(f)
+        tot_p += npr
+        a += width
+    dt = time.perf_counter() - t
+    value = args.steps * width / dt
+    sample = (f"{args.steps} steps of {width}-wide windows of the workload from 1e13 "
+              f"({tot_p} primes, {tot_f} factors)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "sample_width": width},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference sieve (kernel_v0.24.6.cu) has no CPU path; this arm is the scalar "
+                 "CPU BSGS oracle restating it, all host threads"),
+    }))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--slice", type=float, default=SLICE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+
+    import rsieve
+    import rsieve.synth as S
+
+    rsieve.build()
+    dist = Dist(world, local, "nccl")
+    dev = local
+    slice_w = int(args.slice)
+    job_args = S.plain_job(1)
+    b, s, ks, nl = job_args
+    abcd = S.to_abcd(b, s, ks, nl)
+
+    # roofline denominator: this GPU's integer-multiply throughput
+    mul_ops, mont_per_s = rsieve.bench_imad(dev)
+
+    job = rsieve.Job(base=b, sign=s, ks=ks, nlists=nl, device=dev)
+    info = job.info
+    # warm-up: slices just below the window
+    for w in range(args.warmup):
+        a = P_START - (w + 1) * (slice_w // 10)
+        job.sieve(a, a + slice_w // 10 - 1)
+
+    sampler = ClockSampler(dev)
+    dist.barrier()
+    sampler.start()
+    t0 = time.perf_counter()
+    gpu_ms = bsgs_ms = 0.0
+    primes = launches = bsgs_launches = factors = 0
+    for step in range(args.steps):
+        idx = step * world + rank
+        a = P_START + idx * slice_w
+        f, st = job.sieve(a, a + slice_w - 1)
+        gpu_ms += st["gpu_ms"]
+        bsgs_ms += st["bsgs_ms"]
+        primes += st["primes"]
+        launches += st["launches"]
+        bsgs_launches += st["bsgs_launches"]
+        factors += len(f)
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    dist.barrier()
+    job.close()
+    t_max = dist.max(gpu_ms / 1e3)
+    total_width = world * args.steps * slice_w
+    value = total_width / t_max
+
+    # roofline of the BSGS kernel: algorithmic multiply ops / BSGS kernel time
+    alg_ops = primes * info["work_per_prime"] * MONTMUL_MULS
+    achieved = alg_ops / (bsgs_ms / 1e3) / 1e12
+    peak = mont_per_s * MONTMUL_MULS / 1e12
+
+    e2e = None
+    if not args.no_e2e:
+        dist.barrier()
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        e2e_steps = max(1, min(args.steps, 3))
+        for step in range(e2e_steps):
+            idx = step * world + rank
+            a = P_START + idx * slice_w
+            with rsieve.Job(abcd, device=dev) as j2:
+                f, st = j2.sieve(a, a + slice_w - 1)
+                h2d += j2.info["upload_bytes"] + st["h2d_bytes"]
+                d2h += st["d2h_bytes"]
+        e2e_t = dist.max(time.perf_counter() - t0)
+        e2e = {"value": world * e2e_steps * slice_w / e2e_t, "unit": UNIT,
+               "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+               "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(job_args)
+    dist.close()
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": gpu_ms / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
+        "config": {
+            "workload": WORKLOAD, "slice_width": slice_w, "plan": {
+                k: info[k] for k in ("Q", "rows", "x_range", "baby_steps", "giant_steps", "table_slots",
+                                     "primes_per_launch")},
+            "l2": "no flush: each step streams ~2.7 GB of fresh prime windows (> 129 MB L2); the 0.2 MB "
+                  "job tables stay resident by design",
+            "parallelism": f"p-range shards x{world}, no collective",
+        },
+        "roofline": {
+            "bound": "imad", "achieved": achieved, "peak": peak, "unit": "Tops/s", "frac": achieved / peak,
+            "traffic": None,
+            "what": ("32-bit multiply-class ops of the algorithmic BSGS work (2*sqrt(E[R]*X) Montgomery "
+                     f"products per prime = {info['work_per_prime']:.0f}, x{MONTMUL_MULS} ops) per second of "
+                     "BSGS kernel time"),
+            "peak_source": ("measured this run by rs_bench_imad: independent Montgomery-product chains "
+                            f"({mont_per_s:.3e}/s x{MONTMUL_MULS}); plain mad.lo.u32 peak "
+                            f"{mul_ops / 1e12:.1f} Tops/s"),
+        },
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "detail": {"primes": primes, "factors": factors, "bsgs_ms": bsgs_ms, "gpu_ms": gpu_ms,
+                   "wall_s": wall, "bsgs_launches": bsgs_launches,
+                   "bsgs_share": bsgs_ms / gpu_ms if gpu_ms else None},
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

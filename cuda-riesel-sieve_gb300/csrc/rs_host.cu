@@ -1,0 +1,983 @@
+// rs_host.cu -- host side of librsieve_gb300: ABCD input, planner, device
+// resources, the p-range driver loop and the C ABI declared in include/rsieve.h.
+//
+// Reference counterparts (rob147147/CUDA-Riesel-Sieve, kernel_v0.24.6.cu):
+//   ABCD reader            938-1083   -> parse_abcd
+//   Q choice / rows        1086-1255  -> make_plan (cost model instead of rows*range)
+//   device setup, upload   1367-1512  -> upload_job / ensure_chunk_buffers
+//   driver loop            1537-1770  -> rs_sieve_range (no overshoot past P1,
+//                                        chunks pipelined on one stream, one sync)
+//   verify + write         1600-1732, 1830-1835 -> verify kernel, host_verify,
+//                                        rs_write_factors
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rs_internal.h"
+#include "rsieve.h"
+
+using namespace rs;
+
+// ---------------------------------------------------------------------------
+// Errors
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                   \
+  do {                                                                                   \
+    cudaError_t _e = (expr);                                                             \
+    if (_e != cudaSuccess)                                                               \
+      return fail(_e == cudaErrorMemoryAllocation ? RS_ERR_NOMEM : RS_ERR_CUDA, "%s: %s", \
+                  #expr, cudaGetErrorString(_e));                                        \
+  } while (0)
+
+static int check_device(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= 0)
+    return fail(RS_ERR_NODEVICE, "no CUDA device available (%s); this library has no CPU path",
+                e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+  if (device < 0 || device >= n) return fail(RS_ERR_INVALID, "device %d out of range [0,%d)", device, n);
+  CUDA_TRY(cudaSetDevice(device));
+  return RS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// ABCD input (kernel_v0.24.6.cu:938-1083): "ABCD k*b^$a-1 [n0]" headers followed
+// by positive n deltas.  Unlike the reference this rejects malformed lines,
+// takes the sign from the header and merges repeated k.
+
+struct Seqs {
+  uint32_t base = 0;
+  int32_t sign = 0;
+  std::vector<uint32_t> k;
+  std::vector<std::vector<uint32_t>> n;
+};
+
+static int parse_abcd(const char *text, size_t len, Seqs &out) {
+  size_t i = 0;
+  long line = 0;
+  uint64_t total = 0;
+  while (i < len) {
+    size_t e = i;
+    while (e < len && text[e] != '\n') e++;
+    line++;
+    size_t a = i, z = e;
+    i = e + 1;
+    while (z > a && (text[z - 1] == '\r' || text[z - 1] == ' ' || text[z - 1] == '\t')) z--;
+    while (a < z && (text[a] == ' ' || text[a] == '\t')) a++;
+    if (a == z) continue;
+    std::string s(text + a, z - a);
+    if (s.compare(0, 4, "ABCD") == 0 && s.size() > 4 && (s[4] == ' ' || s[4] == '\t')) {
+      const char *c = s.c_str() + 5;
+      while (*c == ' ' || *c == '\t') c++;
+      char *end;
+      unsigned long long kv = strtoull(c, &end, 10);
+      if (end == c || *end != '*' || kv == 0 || kv > 0xffffffffull)
+        return fail(RS_ERR_INVALID, "ABCD line %ld: bad k in header", line);
+      c = end + 1;
+      unsigned long long bv = strtoull(c, &end, 10);
+      if (end == c || *end != '^' || bv < 2 || bv > 0xffffffffull)
+        return fail(RS_ERR_INVALID, "ABCD line %ld: bad base in header", line);
+      const char *dol = strstr(end, "$a");
+      if (!dol) return fail(RS_ERR_INVALID, "ABCD line %ld: expected $a exponent", line);
+      int32_t sg;
+      if (dol[2] == '-' && dol[3] == '1') sg = -1;
+      else if (dol[2] == '+' && dol[3] == '1') sg = +1;
+      else return fail(RS_ERR_INVALID, "ABCD line %ld: expected -1 or +1", line);
+      const char *lb = strchr(dol, '[');
+      if (!lb) return fail(RS_ERR_INVALID, "ABCD line %ld: missing [n0]", line);
+      long long n0 = strtoll(lb + 1, &end, 10);
+      if (end == lb + 1 || *end != ']' || n0 < 0 || n0 > 0x7fffffffll)
+        return fail(RS_ERR_INVALID, "ABCD line %ld: bad [n0]", line);
+      if (out.base == 0) {
+        out.base = (uint32_t)bv;
+        out.sign = sg;
+      } else if (bv != out.base) {
+        return fail(RS_ERR_INVALID, "ABCD line %ld: all sequences must share one base", line);
+      } else if (sg != out.sign) {
+        return fail(RS_ERR_INVALID, "ABCD line %ld: all sequences must share one sign", line);
+      }
+      out.k.push_back((uint32_t)kv);
+      out.n.emplace_back();
+      out.n.back().push_back((uint32_t)n0);
+      total = (uint64_t)n0;
+    } else {
+      if (out.k.empty())
+        return fail(RS_ERR_INVALID, "ABCD line %ld: data before the first ABCD header", line);
+      char *end;
+      long long d = strtoll(s.c_str(), &end, 10);
+      if (end == s.c_str() || d <= 0) return fail(RS_ERR_INVALID, "ABCD line %ld: bad n delta", line);
+      total += (uint64_t)d;
+      if (total > 0x7fffffffull) return fail(RS_ERR_INVALID, "ABCD line %ld: n exceeds 2^31-1", line);
+      out.n.back().push_back((uint32_t)total);
+    }
+  }
+  if (out.k.empty()) return fail(RS_ERR_INVALID, "no ABCD header found");
+  return RS_OK;
+}
+
+// Merge repeated k, sort and de-duplicate every n list.
+static void normalise(Seqs &s) {
+  Seqs o;
+  o.base = s.base;
+  o.sign = s.sign;
+  for (size_t i = 0; i < s.k.size(); i++) {
+    size_t j = 0;
+    for (; j < o.k.size(); j++)
+      if (o.k[j] == s.k[i]) break;
+    if (j == o.k.size()) {
+      o.k.push_back(s.k[i]);
+      o.n.push_back(std::move(s.n[i]));
+    } else {
+      o.n[j].insert(o.n[j].end(), s.n[i].begin(), s.n[i].end());
+    }
+  }
+  for (auto &v : o.n) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+  }
+  s = std::move(o);
+}
+
+// ---------------------------------------------------------------------------
+// Planner.  The reference picks the even Q in [2,22] minimising rows*range and
+// keeps Q=1 unless strictly cheaper (kernel_v0.24.6.cu:1086-1146).  Here the
+// cost is the per-lane Montgomery-product count of the warp-per-prime kernel;
+// Q, the giant steps per row T and the baby steps m are chosen together.
+
+struct Plan {
+  uint32_t Q = 0, nrows = 0, X = 0, x_lo = 0, x_hi = 0, m = 0, T = 0;
+  uint32_t tlanes = 0, rows_per_it = 0, steps_per_lane = 0, table_log2 = 0, jbits = 0;
+  uint32_t nmin = 0, nmax = 0, ncand = 0, words_per_row = 0;
+  int64_t e0 = 0;
+  double cost = 0, work_per_prime = 0;
+  std::vector<uint32_t> row_r, row_kidx, k_row0;
+  std::vector<uint32_t> bitmap;
+};
+
+static uint32_t ilog2_ceil(uint64_t v) {
+  uint32_t b = 0;
+  while (((uint64_t)1 << b) < v) b++;
+  return b;
+}
+
+static constexpr uint32_t kMaxTableLog2 = 13;  // 8192 slots = 32 KB per warp
+
+static int count_rows(const Seqs &s, uint32_t Q, bool datless) {
+  if (datless) return (int)(s.k.size() * Q);
+  int rows = 0;
+  std::vector<char> seen(Q);
+  for (size_t i = 0; i < s.k.size(); i++) {
+    std::fill(seen.begin(), seen.end(), 0);
+    for (uint32_t n : s.n[i])
+      if (!seen[n % Q]) {
+        seen[n % Q] = 1;
+        rows++;
+      }
+  }
+  return rows;
+}
+
+static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
+  uint32_t nmin = 0xffffffffu, nmax = 0, ncand = 0;
+  for (auto &v : s.n) {
+    if (v.empty()) continue;
+    nmin = std::min(nmin, v.front());
+    nmax = std::max(nmax, v.back());
+    ncand += (uint32_t)v.size();
+  }
+  if (ncand == 0) return fail(RS_ERR_INVALID, "job has no candidates");
+  const bool datless = opt.datless != 0;
+  const double K = (double)s.k.size();
+  std::vector<uint32_t> Qs;
+  if (opt.Q > 0) {
+    Qs.push_back((uint32_t)opt.Q);
+  } else {
+    Qs.push_back(1);
+    for (uint32_t q = 2; q <= 48; q += 2) Qs.push_back(q);
+  }
+  uint64_t mcap = 65534;
+  if (opt.hash_m > 0) {
+    if (opt.hash_m > 14) return fail(RS_ERR_INVALID, "-m %d too large (at most 14)", opt.hash_m);
+    mcap = std::min<uint64_t>(mcap, (uint64_t)2 << opt.hash_m);
+  }
+  double best = 1e300;
+  for (uint32_t Q : Qs) {
+    const uint32_t X = nmax / Q - nmin / Q + 1;
+    const int rows = count_rows(s, Q, datless);
+    const double ER = rows * ((Q & 1) ? 0.75 : 0.5);
+    for (uint32_t tl = 0; tl <= 20; tl++) {
+      const uint64_t T = (uint64_t)1 << tl;
+      const uint64_t m = (X + T - 1) / T;
+      if (m > mcap) continue;
+      if (m * T < X) continue;
+      const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));
+      if (slog > kMaxTableLog2) continue;
+      const uint32_t tlanes = (uint32_t)std::min<uint64_t>(T, 32);
+      const uint32_t rpi = 32 / tlanes;
+      const uint32_t spl = (uint32_t)std::max<uint64_t>(1, T / 32);
+      double cost = std::ceil((double)m / 32.0) + std::ceil(ER / rpi) * spl +
+                    (double)(1u << slog) / 512.0 +
+                    (K * (2.0 + Q / 2.0) + ER + 63.0 + 40.0) / 32.0;
+      if (cost < best) {
+        best = cost;
+        pl.Q = Q;
+        pl.nrows = (uint32_t)rows;
+        pl.X = X;
+        pl.m = (uint32_t)m;
+        pl.T = (uint32_t)T;
+        pl.tlanes = tlanes;
+        pl.rows_per_it = rpi;
+        pl.steps_per_lane = spl;
+        pl.table_log2 = slog;
+        pl.cost = cost;
+        pl.work_per_prime = 2.0 * std::sqrt(ER * (double)X);
+      }
+    }
+  }
+  if (pl.Q == 0) return fail(RS_ERR_INVALID, "no feasible plan (n range too wide for the -m limit)");
+  pl.nmin = nmin;
+  pl.nmax = nmax;
+  pl.ncand = ncand;
+  pl.x_lo = nmin / pl.Q;
+  pl.x_hi = nmax / pl.Q;
+  pl.e0 = (int64_t)pl.x_lo - 1;
+  pl.jbits = 1;
+  while (((uint64_t)1 << pl.jbits) < (uint64_t)pl.m + 1) pl.jbits++;
+  pl.words_per_row = (pl.X + 31) / 32;
+  // rows: k in input order, r ascending
+  const uint32_t Q = pl.Q;
+  pl.k_row0.assign(s.k.size() + 1, 0);
+  std::vector<int> rid(Q);
+  for (size_t i = 0; i < s.k.size(); i++) {
+    pl.k_row0[i] = (uint32_t)pl.row_r.size();
+    std::fill(rid.begin(), rid.end(), -1);
+    if (datless) {
+      for (uint32_t r = 0; r < Q; r++) rid[r] = 1;
+    } else {
+      for (uint32_t n : s.n[i]) rid[n % Q] = 1;
+    }
+    for (uint32_t r = 0; r < Q; r++)
+      if (rid[r] >= 0) {
+        rid[r] = (int)pl.row_r.size();
+        pl.row_r.push_back(r);
+        pl.row_kidx.push_back((uint32_t)i);
+      }
+    if (!datless) {
+      // candidate bitmap rows (bits for x - x_lo)
+      size_t base_words = pl.bitmap.size();
+      size_t nr = pl.row_r.size() - pl.k_row0[i];
+      pl.bitmap.resize(base_words + nr * pl.words_per_row, 0);
+      for (uint32_t n : s.n[i]) {
+        const uint32_t r = n % Q;
+        const uint32_t row_local = (uint32_t)rid[r] - pl.k_row0[i];
+        const uint32_t bit = n / Q - pl.x_lo;
+        pl.bitmap[base_words + (size_t)row_local * pl.words_per_row + bit / 32] |= 1u << (bit & 31);
+      }
+    }
+  }
+  pl.k_row0[s.k.size()] = (uint32_t)pl.row_r.size();
+  pl.nrows = (uint32_t)pl.row_r.size();
+  if (datless) pl.bitmap.assign(1, 0);
+  return RS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The job.
+
+struct rs_job {
+  std::mutex mu;
+  rs_options opt;
+  Seqs seqs;
+  Plan plan;
+  JobDev dev{};
+  int device = 0;
+  cudaStream_t st = nullptr;
+  void *d_job = nullptr;  // job arrays
+  size_t job_bytes = 0;
+  // sieving primes (odd primes <= sp_limit)
+  uint64_t sp_limit = 0;
+  uint32_t nsp = 0;
+  uint32_t *d_sp = nullptr;
+  uint64_t *d_sp_rcp = nullptr;
+  // chunk and hit buffers
+  ChunkBufs cb{};
+  void *d_chunk = nullptr;
+  HitBufs hb{};
+  void *d_hits = nullptr;
+  uint32_t *h_counts = nullptr;  // pinned, one slot per chunk + 2
+  size_t h_counts_cap = 0;
+  int bsgs_grid = 0;
+  uint32_t chunk_cap = 0;
+};
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static int upload_job(rs_job *j) {
+  const Plan &pl = j->plan;
+  const Seqs &s = j->seqs;
+  const uint32_t nk = (uint32_t)s.k.size();
+  std::vector<uint32_t> kodd(nk), ke2(nk);
+  std::vector<uint64_t> krcp(nk);
+  for (uint32_t i = 0; i < nk; i++) {
+    uint32_t k = s.k[i], e = 0;
+    while (!(k & 1)) {
+      k >>= 1;
+      e++;
+    }
+    kodd[i] = k;
+    ke2[i] = e;
+    krcp[i] = k > 1 ? (~0ull) / k : 0;
+  }
+  // one allocation, 256-byte aligned sections
+  size_t off = 0;
+  auto sec = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4);
+  const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
+  const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
+  j->job_bytes = off;
+  std::vector<uint8_t> host(off, 0);
+  memcpy(host.data() + o_rr, pl.row_r.data(), pl.row_r.size() * 4);
+  memcpy(host.data() + o_rk, pl.row_kidx.data(), pl.row_kidx.size() * 4);
+  memcpy(host.data() + o_kv, s.k.data(), nk * 4);
+  memcpy(host.data() + o_ko, kodd.data(), nk * 4);
+  memcpy(host.data() + o_ke, ke2.data(), nk * 4);
+  memcpy(host.data() + o_kr, krcp.data(), nk * 8);
+  memcpy(host.data() + o_k0, pl.k_row0.data(), (nk + 1) * 4);
+  memcpy(host.data() + o_bm, pl.bitmap.data(), pl.bitmap.size() * 4);
+  CUDA_TRY(cudaMalloc(&j->d_job, off));
+  CUDA_TRY(cudaMemcpyAsync(j->d_job, host.data(), off, cudaMemcpyHostToDevice, j->st));
+  CUDA_TRY(cudaStreamSynchronize(j->st));
+  uint8_t *b = (uint8_t *)j->d_job;
+  JobDev &d = j->dev;
+  d.base = s.base;
+  d.sign = s.sign;
+  d.Q = pl.Q;
+  d.m = pl.m;
+  d.T = pl.T;
+  d.tlanes = pl.tlanes;
+  d.rows_per_it = pl.rows_per_it;
+  d.steps_per_lane = pl.steps_per_lane;
+  d.table_log2 = pl.table_log2;
+  d.jbits = pl.jbits;
+  d.nrows = pl.nrows;
+  d.nk = nk;
+  d.e0 = pl.e0;
+  d.x_lo = pl.x_lo;
+  d.x_hi = pl.x_hi;
+  d.nmin = pl.nmin;
+  d.nmax = pl.nmax;
+  d.words_per_row = pl.words_per_row;
+  d.datless = j->opt.datless ? 1u : 0u;
+  d.max_act = std::max<uint32_t>(1, pl.nrows);
+  d.row_r = (const uint32_t *)(b + o_rr);
+  d.row_kidx = (const uint32_t *)(b + o_rk);
+  d.k_val = (const uint32_t *)(b + o_kv);
+  d.k_odd = (const uint32_t *)(b + o_ko);
+  d.k_e2 = (const uint32_t *)(b + o_ke);
+  d.k_rcp = (const uint64_t *)(b + o_kr);
+  d.k_row0 = (const uint32_t *)(b + o_k0);
+  d.bitmap = (const uint32_t *)(b + o_bm);
+  uint32_t bb = s.base, be = 0;
+  while (!(bb & 1)) {
+    bb >>= 1;
+    be++;
+  }
+  d.b_odd = bb;
+  d.b_e2 = be;
+  d.b_rcp = bb > 1 ? (~0ull) / bb : 0;
+  return RS_OK;
+}
+
+// Odd primes <= limit by a simple sieve (the reference builds its small-prime
+// table on the host too, kernel_v0.24.6.cu:1271-1303).
+static int ensure_sieving_primes(rs_job *j, uint64_t hi, uint64_t *h2d = nullptr) {
+  uint64_t r = (uint64_t)std::sqrt((long double)hi);
+  while (r * r > hi) r--;
+  while ((r + 1) * (r + 1) <= hi) r++;
+  if (j->d_sp && r <= j->sp_limit) return RS_OK;
+  uint64_t limit = std::max<uint64_t>(r, std::min<uint64_t>(2 * r, 1ull << 22));
+  std::vector<uint8_t> comp(limit / 2 + 1, 0);
+  std::vector<uint32_t> ps;
+  std::vector<uint64_t> rc;
+  for (uint64_t i = 3; i <= limit; i += 2) {
+    if (comp[i / 2]) continue;
+    ps.push_back((uint32_t)i);
+    rc.push_back((~0ull) / i);
+    for (uint64_t q = i * i; q <= limit; q += 2 * i) comp[q / 2] = 1;
+  }
+  if (j->d_sp) cudaFree(j->d_sp);
+  if (j->d_sp_rcp) cudaFree(j->d_sp_rcp);
+  j->d_sp = nullptr;
+  j->d_sp_rcp = nullptr;
+  CUDA_TRY(cudaMalloc(&j->d_sp, std::max<size_t>(1, ps.size()) * 4));
+  CUDA_TRY(cudaMalloc(&j->d_sp_rcp, std::max<size_t>(1, rc.size()) * 8));
+  CUDA_TRY(cudaMemcpyAsync(j->d_sp, ps.data(), ps.size() * 4, cudaMemcpyHostToDevice, j->st));
+  CUDA_TRY(cudaMemcpyAsync(j->d_sp_rcp, rc.data(), rc.size() * 8, cudaMemcpyHostToDevice, j->st));
+  CUDA_TRY(cudaStreamSynchronize(j->st));
+  j->nsp = (uint32_t)ps.size();
+  j->sp_limit = limit;
+  if (h2d) *h2d += ps.size() * 12;
+  return RS_OK;
+}
+
+static size_t chunk_bytes_per_prime(const rs_job *j) {
+  return 8 + sizeof(PrimeRec) + 32 * 8 * 2 + (size_t)j->dev.max_act * 12;
+}
+
+static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
+  if (j->d_chunk && j->chunk_cap >= cap) return RS_OK;
+  if (j->d_chunk) cudaFree(j->d_chunk);
+  j->d_chunk = nullptr;
+  size_t off = 0;
+  auto sec = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * sizeof(PrimeRec));
+  const size_t o_vb = sec((size_t)cap * 256), o_vg = sec((size_t)cap * 256);
+  const size_t o_av = sec((size_t)cap * j->dev.max_act * 8), o_ar = sec((size_t)cap * j->dev.max_act * 4);
+  CUDA_TRY(cudaMalloc(&j->d_chunk, off));
+  uint8_t *b = (uint8_t *)j->d_chunk;
+  j->cb.primes = (uint64_t *)(b + o_pr);
+  j->cb.count = (uint32_t *)(b + o_ct);
+  j->cb.rec = (PrimeRec *)(b + o_rec);
+  j->cb.vecB = (uint64_t *)(b + o_vb);
+  j->cb.vecG = (uint64_t *)(b + o_vg);
+  j->cb.actV = (uint64_t *)(b + o_av);
+  j->cb.actRow = (uint32_t *)(b + o_ar);
+  j->cb.cap = cap;
+  j->chunk_cap = cap;
+  return RS_OK;
+}
+
+static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
+  if (j->d_hits && j->hb.cap >= cap) return RS_OK;
+  if (j->d_hits) cudaFree(j->d_hits);
+  j->d_hits = nullptr;
+  size_t off = 0;
+  auto sec = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  const size_t o_raw = sec((size_t)cap * sizeof(Hit)), o_rc = sec(16);
+  const size_t o_fac = sec((size_t)cap * sizeof(Hit)), o_fc = sec(16);
+  CUDA_TRY(cudaMalloc(&j->d_hits, off));
+  uint8_t *b = (uint8_t *)j->d_hits;
+  j->hb.raw = (Hit *)(b + o_raw);
+  j->hb.raw_count = (uint32_t *)(b + o_rc);
+  j->hb.fac = (Hit *)(b + o_fac);
+  j->hb.fac_count = (uint32_t *)(b + o_fc);
+  j->hb.cap = cap;
+  return RS_OK;
+}
+
+static void free_job(rs_job *j) {
+  if (!j) return;
+  if (j->st) cudaStreamSynchronize(j->st);
+  if (j->d_job) cudaFree(j->d_job);
+  if (j->d_sp) cudaFree(j->d_sp);
+  if (j->d_sp_rcp) cudaFree(j->d_sp_rcp);
+  if (j->d_chunk) cudaFree(j->d_chunk);
+  if (j->d_hits) cudaFree(j->d_hits);
+  if (j->h_counts) cudaFreeHost(j->h_counts);
+  if (j->st) cudaStreamDestroy(j->st);
+  delete j;
+}
+
+static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out) {
+  if (!out) return fail(RS_ERR_INVALID, "job pointer is NULL");
+  *out = nullptr;
+  rs_options opt;
+  if (optp) opt = *optp;
+  else rs_options_default(&opt);
+  normalise(seqs);
+  if (seqs.sign != -1 && seqs.sign != 1) return fail(RS_ERR_INVALID, "sign must be -1 or +1");
+  if (seqs.base < 2) return fail(RS_ERR_INVALID, "base must be >= 2");
+  if (opt.Q < 0 || opt.Q > 4096) return fail(RS_ERR_INVALID, "Q must be in [0, 4096]");
+  if (opt.block_scale < 0 || opt.block_scale > 31 || opt.thread_scale < 0 || opt.thread_scale > 31)
+    return fail(RS_ERR_INVALID, "-b/-t scale must be in [1, 31]");
+  Plan pl;
+  int rc = make_plan(seqs, opt, pl);
+  if (rc) return rc;
+  rc = check_device(opt.device);
+  if (rc) return rc;
+  rs_job *j = new rs_job();
+  j->opt = opt;
+  j->seqs = std::move(seqs);
+  j->plan = std::move(pl);
+  j->device = opt.device;
+  cudaError_t e = cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete j;
+    return fail(RS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  rc = upload_job(j);
+  if (!rc) {
+    e = bsgs_configure(j->dev, j->device, &j->bsgs_grid);
+    if (e != cudaSuccess) rc = fail(RS_ERR_CUDA, "bsgs_configure: %s", cudaGetErrorString(e));
+  }
+  if (rc) {
+    free_job(j);
+    return rc;
+  }
+  // primes per launch: -b/-t as in the reference (128*2^(b-1) blocks of
+  // 128*2^(t-1) threads, one prime each), else a memory budget of ~2 GB.
+  uint64_t cap;
+  if (opt.block_scale > 0 || opt.thread_scale > 0) {
+    const int bs = opt.block_scale > 0 ? opt.block_scale : 1, ts = opt.thread_scale > 0 ? opt.thread_scale : 1;
+    cap = (uint64_t)128 << (bs - 1);
+    cap *= (uint64_t)128 << (ts - 1);
+  } else {
+    cap = (2ull << 30) / chunk_bytes_per_prime(j);
+  }
+  cap = std::max<uint64_t>(cap, 4096);
+  cap = std::min<uint64_t>(cap, 1u << 23);
+  j->chunk_cap = 0;
+  j->cb.cap = (uint32_t)cap;
+  *out = j;
+  return RS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host re-verification, 128-bit arithmetic (kernel_v0.24.6.cu:1649-1671).
+
+static bool host_verify(uint64_t p, uint32_t k, uint32_t b, uint32_t n, int32_t sign) {
+  typedef unsigned __int128 u128;
+  u128 val = 1;
+  const uint64_t bb = b % p;
+  for (int z = 31; z >= 0; --z) {
+    val = (val * val) % p;
+    if (n & (1u << z)) val = (val * bb) % p;
+  }
+  val = (val * (k % p)) % p;
+  return (uint64_t)val == (sign < 0 ? 1 % p : p - 1);
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+void rs_options_default(rs_options *opt) {
+  if (!opt) return;
+  memset(opt, 0, sizeof(*opt));
+  opt->host_verify = 1;
+}
+
+const char *rs_last_error(void) { return g_err.c_str(); }
+
+const char *rs_version(void) { return "rsieve-gb300 0.1.0 (sm_103a)"; }
+
+int rs_job_create_abcd(const char *text, size_t len, const rs_options *opt, rs_job **job) {
+  if (!text) return fail(RS_ERR_INVALID, "ABCD text is NULL");
+  Seqs s;
+  int rc = parse_abcd(text, len, s);
+  if (rc) return rc;
+  return create_from_seqs(std::move(s), opt, job);
+}
+
+int rs_job_create(uint32_t base, int32_t sign, uint32_t num_k, const uint32_t *k,
+                  const uint32_t *n_offsets, const uint32_t *n_values, const rs_options *opt,
+                  rs_job **job) {
+  if (num_k == 0 || !k || !n_offsets || !n_values) return fail(RS_ERR_INVALID, "empty job");
+  Seqs s;
+  s.base = base;
+  s.sign = sign;
+  for (uint32_t i = 0; i < num_k; i++) {
+    if (k[i] == 0) return fail(RS_ERR_INVALID, "k must be positive");
+    if (n_offsets[i + 1] < n_offsets[i]) return fail(RS_ERR_INVALID, "n_offsets not ascending");
+    s.k.push_back(k[i]);
+    s.n.emplace_back(n_values + n_offsets[i], n_values + n_offsets[i + 1]);
+    for (uint32_t v : s.n.back())
+      if (v > 0x7fffffffu) return fail(RS_ERR_INVALID, "n exceeds 2^31-1");
+  }
+  return create_from_seqs(std::move(s), opt, job);
+}
+
+int rs_job_info_get(const rs_job *j, rs_job_info *info) {
+  if (!j || !info) return fail(RS_ERR_INVALID, "NULL argument");
+  const Plan &pl = j->plan;
+  info->base = j->seqs.base;
+  info->sign = j->seqs.sign;
+  info->num_k = (uint32_t)j->seqs.k.size();
+  info->num_candidates = pl.ncand;
+  info->nmin = pl.nmin;
+  info->nmax = pl.nmax;
+  info->Q = pl.Q;
+  info->rows = pl.nrows;
+  info->x_range = pl.X;
+  info->baby_steps = pl.m;
+  info->giant_steps = pl.T;
+  info->table_slots = 1u << pl.table_log2;
+  info->primes_per_launch = j->cb.cap;
+  info->work_per_prime = pl.work_per_prime;
+  info->upload_bytes = j->job_bytes;
+  return RS_OK;
+}
+
+int rs_job_destroy(rs_job *j) {
+  if (!j) return RS_OK;
+  cudaSetDevice(j->device);
+  free_job(j);
+  return RS_OK;
+}
+
+}  // extern "C"
+
+static constexpr int kRetryHits = -1;
+
+// One pass over [p0, p1]; returns kRetryHits after growing the hit buffers
+// when more candidate hits arrived than they could hold.
+static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
+                            size_t *count, rs_stats *stats) {
+  *count = 0;
+  rs_stats st;
+  memset(&st, 0, sizeof(st));
+  if (p1 >= (1ull << 63)) return fail(RS_ERR_RANGE, "p1 must be < 2^63");
+  uint64_t lo = p0 < 3 ? 3 : p0;
+  if (!(lo & 1)) lo++;
+  const uint64_t hi = p1;
+  if (lo > hi) {
+    if (stats) *stats = st;
+    return RS_OK;
+  }
+  CUDA_TRY(cudaSetDevice(j->device));
+  int rc = ensure_sieving_primes(j, hi, &st.h2d_bytes);
+  if (rc) return rc;
+  rc = ensure_chunk_buffers(j, j->cb.cap);
+  if (rc) return rc;
+  if (!j->d_hits) {
+    rc = ensure_hit_buffers(j, 1u << 20);
+    if (rc) return rc;
+  }
+  const uint32_t C = j->cb.cap;
+
+  // chunk list [a, b] with expected prime count ~0.8*C
+  struct Chunk {
+    uint64_t a, b;
+  };
+  std::vector<Chunk> todo;
+  {
+    uint64_t a = lo;
+    while (a <= hi) {
+      const double la = std::log((double)a);
+      double w = la > 3.0 ? 0.8 * (double)C * (la - 1.2) : 1.6 * (double)C;
+      if (w < 64) w = 64;
+      uint64_t width = (uint64_t)w & ~1ull;
+      uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
+      todo.push_back({a, b});
+      if (b >= hi) break;
+      a = b + 1;
+      if (!(a & 1)) a++;
+    }
+  }
+
+  cudaEvent_t ev0, ev1;
+  CUDA_TRY(cudaEventCreate(&ev0));
+  CUDA_TRY(cudaEventCreate(&ev1));
+  std::vector<cudaEvent_t> evs;
+  auto cleanup_events = [&]() {
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    for (auto e : evs) cudaEventDestroy(e);
+  };
+  bool first_pass = true;
+  uint64_t total_primes = 0;
+  for (int attempt = 0; attempt < 8 && !todo.empty(); attempt++) {
+    if (j->h_counts_cap < todo.size() + 2) {
+      if (j->h_counts) cudaFreeHost(j->h_counts);
+      j->h_counts = nullptr;
+      j->h_counts_cap = todo.size() + 2;
+      cudaError_t e = cudaMallocHost(&j->h_counts, j->h_counts_cap * 4);
+      if (e != cudaSuccess) {
+        cleanup_events();
+        return fail(RS_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e));
+      }
+    }
+    // (re)create timing events: 6 per chunk
+    while (evs.size() < todo.size() * 6) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) break;
+      evs.push_back(e);
+    }
+    const bool timed = evs.size() >= todo.size() * 6;
+    if (first_pass) {
+      cudaMemsetAsync(j->hb.raw_count, 0, 4, j->st);
+      cudaMemsetAsync(j->hb.fac_count, 0, 4, j->st);
+      cudaEventRecord(ev0, j->st);
+    }
+    for (size_t c = 0; c < todo.size(); c++) {
+      cudaMemsetAsync(j->cb.count, 0, 4, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 0], j->st);
+      cudaError_t e = launch_sieve(todo[c].a, todo[c].b, j->d_sp, j->d_sp_rcp, j->nsp, j->cb.primes,
+                                   j->cb.count, C, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 1], j->st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
+      if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 3], j->st);
+      if (e == cudaSuccess) e = launch_bsgs(j->dev, j->cb, j->hb, j->bsgs_grid, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 4], j->st);
+      if (e != cudaSuccess) {
+        cleanup_events();
+        return fail(RS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+      }
+      st.launches += 3;
+      st.bsgs_launches += 1;
+    }
+    cudaError_t e = cudaStreamSynchronize(j->st);
+    if (e != cudaSuccess) {
+      cleanup_events();
+      return fail(RS_ERR_CUDA, "sieve kernels: %s", cudaGetErrorString(e));
+    }
+    st.d2h_bytes += 4 * todo.size();
+    if (timed) {
+      for (size_t c = 0; c < todo.size(); c++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, evs[6 * c + 0], evs[6 * c + 1]);
+        st.sieve_ms += ms;
+        cudaEventElapsedTime(&ms, evs[6 * c + 2], evs[6 * c + 3]);
+        st.setup_ms += ms;
+        cudaEventElapsedTime(&ms, evs[6 * c + 3], evs[6 * c + 4]);
+        st.bsgs_ms += ms;
+      }
+    }
+    std::vector<Chunk> redo;
+    for (size_t c = 0; c < todo.size(); c++) {
+      const uint32_t n = j->h_counts[c];
+      if (n > C) {
+        // more primes than the buffer holds: split the chunk and run it again
+        if (todo[c].b - todo[c].a < 8) {
+          cleanup_events();
+          return fail(RS_ERR_INTERNAL, "prime buffer overflow on a tiny chunk");
+        }
+        const uint64_t mid = (todo[c].a + (todo[c].b - todo[c].a) / 2) | 1ull;  // odd, > a
+        redo.push_back({todo[c].a, mid - 1});
+        redo.push_back({mid, todo[c].b});
+      } else {
+        total_primes += n;
+      }
+    }
+    todo.swap(redo);
+    first_pass = false;
+  }
+  if (!todo.empty()) {
+    cleanup_events();
+    return fail(RS_ERR_INTERNAL, "prime buffer overflow could not be resolved");
+  }
+  // verify candidates on the device
+  cudaError_t e = launch_verify(j->dev, j->hb, j->st);
+  st.launches += 1;
+  cudaEventRecord(ev1, j->st);
+  uint32_t counts[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[0], j->hb.raw_count, 4, cudaMemcpyDeviceToHost, j->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[1], j->hb.fac_count, 4, cudaMemcpyDeviceToHost, j->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->st);
+  if (e != cudaSuccess) {
+    cleanup_events();
+    return fail(RS_ERR_CUDA, "verify: %s", cudaGetErrorString(e));
+  }
+  st.d2h_bytes += 8;
+  {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    st.gpu_ms = ms;
+  }
+  cleanup_events();
+  if (counts[0] > j->hb.cap) {
+    const uint64_t need = std::min<uint64_t>((uint64_t)counts[0] * 2, 1u << 30);
+    rc = ensure_hit_buffers(j, (uint32_t)need);
+    return rc ? rc : kRetryHits;
+  }
+  std::vector<Hit> fac(counts[1]);
+  if (counts[1]) {
+    CUDA_TRY(cudaMemcpy(fac.data(), j->hb.fac, counts[1] * sizeof(Hit), cudaMemcpyDeviceToHost));
+    st.d2h_bytes += counts[1] * sizeof(Hit);
+  }
+  std::sort(fac.begin(), fac.end(), [](const Hit &a, const Hit &b) {
+    if (a.p != b.p) return a.p < b.p;
+    if (a.k != b.k) return a.k < b.k;
+    return a.n < b.n;
+  });
+  fac.erase(std::unique(fac.begin(), fac.end(),
+                        [](const Hit &a, const Hit &b) { return a.p == b.p && a.k == b.k && a.n == b.n; }),
+            fac.end());
+  if (j->opt.host_verify) {
+    for (const Hit &h : fac)
+      if (!host_verify(h.p, h.k, j->seqs.base, h.n, j->seqs.sign))
+        return fail(RS_ERR_INTERNAL, "factor %llu | %u*%u^%u%+d failed host verification",
+                    (unsigned long long)h.p, h.k, j->seqs.base, h.n, j->seqs.sign);
+  }
+  st.primes = total_primes;
+  st.raw_hits = counts[0];
+  st.factors = fac.size();
+  st.p_covered = hi - lo + 1;
+  if (stats) *stats = st;
+  *count = fac.size();
+  if (fac.size() > cap) return fail(RS_ERR_CAPACITY, "%zu factors found, buffer holds %zu", fac.size(), cap);
+  for (size_t i = 0; i < fac.size(); i++) {
+    out[i].p = fac[i].p;
+    out[i].k = fac[i].k;
+    out[i].n = fac[i].n;
+  }
+  return RS_OK;
+}
+
+extern "C" int rs_sieve_range(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
+                              size_t *count, rs_stats *stats) {
+  if (!j || !count) return fail(RS_ERR_INVALID, "NULL argument");
+  if (!out && cap) return fail(RS_ERR_INVALID, "NULL output with nonzero capacity");
+  std::lock_guard<std::mutex> lock(j->mu);
+  for (int attempt = 0; attempt < 4; attempt++) {
+    const int rc = sieve_range_impl(j, p0, p1, out, cap, count, stats);
+    if (rc != kRetryHits) return rc;
+  }
+  return fail(RS_ERR_INTERNAL, "candidate-hit buffer overflow could not be resolved");
+}
+
+extern "C" int rs_write_factors(const rs_job *j, const char *path, const rs_factor *f, size_t count) {
+  if (!j || !path || (!f && count)) return fail(RS_ERR_INVALID, "NULL argument");
+  FILE *fp = fopen(path, "a");
+  if (!fp) return fail(RS_ERR_INVALID, "cannot open %s for appending", path);
+  for (size_t i = 0; i < count; i++)
+    fprintf(fp, "%llu | %u*%u^%u%s\n", (unsigned long long)f[i].p, f[i].k, j->seqs.base, f[i].n,
+            j->seqs.sign < 0 ? "-1" : "+1");
+  const int bad = ferror(fp);
+  fclose(fp);
+  if (bad) return fail(RS_ERR_INVALID, "write error on %s", path);
+  return RS_OK;
+}
+
+extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp, rs_job_info *info) {
+  if (!text || !info) return fail(RS_ERR_INVALID, "NULL argument");
+  Seqs s;
+  int rc = parse_abcd(text, len, s);
+  if (rc) return rc;
+  normalise(s);
+  rs_options opt;
+  if (optp) opt = *optp;
+  else rs_options_default(&opt);
+  Plan pl;
+  rc = make_plan(s, opt, pl);
+  if (rc) return rc;
+  memset(info, 0, sizeof(*info));
+  info->base = s.base;
+  info->sign = s.sign;
+  info->num_k = (uint32_t)s.k.size();
+  info->num_candidates = pl.ncand;
+  info->nmin = pl.nmin;
+  info->nmax = pl.nmax;
+  info->Q = pl.Q;
+  info->rows = pl.nrows;
+  info->x_range = pl.X;
+  info->baby_steps = pl.m;
+  info->giant_steps = pl.T;
+  info->table_slots = 1u << pl.table_log2;
+  info->work_per_prime = pl.work_per_prime;
+  return RS_OK;
+}
+
+extern "C" int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *count,
+                             int device) {
+  if (!count || (!out && cap)) return fail(RS_ERR_INVALID, "NULL argument");
+  *count = 0;
+  if (hi >= (1ull << 63)) return fail(RS_ERR_RANGE, "hi must be < 2^63");
+  if (lo < 3) lo = 3;
+  if (!(lo & 1)) lo++;
+  if (lo > hi) return RS_OK;
+  int rc = check_device(device);
+  if (rc) return rc;
+  // a throwaway job-less context: sieving primes + output buffer
+  rs_job tmp;
+  tmp.device = device;
+  CUDA_TRY(cudaStreamCreateWithFlags(&tmp.st, cudaStreamNonBlocking));
+  struct Guard {
+    rs_job &t;
+    uint64_t *d_out = nullptr;
+    uint32_t *d_cnt = nullptr;
+    ~Guard() {
+      if (d_out) cudaFree(d_out);
+      if (d_cnt) cudaFree(d_cnt);
+      if (t.d_sp) cudaFree(t.d_sp);
+      if (t.d_sp_rcp) cudaFree(t.d_sp_rcp);
+      if (t.st) cudaStreamDestroy(t.st);
+      t.d_sp = nullptr;
+      t.d_sp_rcp = nullptr;
+      t.st = nullptr;
+    }
+  } g{tmp};
+  rc = ensure_sieving_primes(&tmp, hi);
+  if (rc) return rc;
+  const uint64_t odds = (hi - lo) / 2 + 1;
+  if (odds > (1ull << 31)) return fail(RS_ERR_RANGE, "rs_gpu_primes: window wider than 2^32");
+  const uint32_t dcap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(odds, std::max<size_t>(cap, 1)));
+  CUDA_TRY(cudaMalloc(&g.d_out, (size_t)dcap * 8));
+  CUDA_TRY(cudaMalloc(&g.d_cnt, 4));
+  CUDA_TRY(cudaMemsetAsync(g.d_cnt, 0, 4, tmp.st));
+  CUDA_TRY(launch_sieve(lo, hi, tmp.d_sp, tmp.d_sp_rcp, tmp.nsp, g.d_out, g.d_cnt, dcap, tmp.st));
+  uint32_t n = 0;
+  CUDA_TRY(cudaMemcpyAsync(&n, g.d_cnt, 4, cudaMemcpyDeviceToHost, tmp.st));
+  CUDA_TRY(cudaStreamSynchronize(tmp.st));
+  *count = n;
+  if (n > cap) return fail(RS_ERR_CAPACITY, "%u primes, buffer holds %zu", n, cap);
+  CUDA_TRY(cudaMemcpy(out, g.d_out, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  std::sort(out, out + n);  // segments finish in any order
+  return RS_OK;
+}
+
+extern "C" int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s) {
+  if (!mul_ops_per_s || !montmul_per_s) return fail(RS_ERR_INVALID, "NULL argument");
+  int rc = check_device(device);
+  if (rc) return rc;
+  CUDA_TRY(run_imad_bench(device, mul_ops_per_s, montmul_per_s));
+  return RS_OK;
+}
+
+extern "C" int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
+                                  uint64_t *out_mulmod, int32_t *out_jacobi_ap, int device) {
+  if (!a || !b || !p || !out_mulmod || !out_jacobi_ap) return fail(RS_ERR_INVALID, "NULL argument");
+  for (size_t i = 0; i < n; i++)
+    if (!(p[i] & 1) || p[i] < 3 || p[i] >= (1ull << 63) || a[i] >= p[i] || b[i] >= p[i])
+      return fail(RS_ERR_INVALID, "arith check input %zu out of range", i);
+  if (n == 0) return RS_OK;
+  int rc = check_device(device);
+  if (rc) return rc;
+  void *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, n * (8 * 4 + 4)));
+  uint64_t *da = (uint64_t *)d, *db = da + n, *dp = db + n, *dm = dp + n;
+  int32_t *dj = (int32_t *)(dm + n);
+  cudaError_t e = cudaMemcpy(da, a, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db, b, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dp, p, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = run_arith_check(da, db, dp, n, dm, dj);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(out_mulmod, dm, n * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(out_jacobi_ap, dj, n * 4, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(RS_ERR_CUDA, "arith check: %s", cudaGetErrorString(e));
+  return RS_OK;
+}

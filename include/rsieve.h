@@ -1,0 +1,155 @@
+/*
+ * rsieve.h -- C ABI of the GB300 Riesel/Sierpinski sieve (librsieve_gb300.so).
+ *
+ * The reference (rob147147/CUDA-Riesel-Sieve, "CUDA Riesel Sieve/kernel_v0.24.6.cu")
+ * exposes no library API: its boundary is the executable's command line plus
+ * the ABCD input file and the factor output file.  Each entry point below
+ * replaces one step of that program, cited as kernel_v0.24.6.cu:LINE, so that
+ * a host (the bundled `rsieve` CLI, a ctypes/cgo/JNI binding) can drive the
+ * sieve without the process-global state the reference keeps
+ * (kernel_v0.24.6.cu:37-52).
+ *
+ * Conventions
+ *   - Every call returns an int status (RS_OK == 0).  On failure,
+ *     rs_last_error() returns a message for the calling thread.
+ *   - A job is caller-owned and immutable once created; device memory belongs
+ *     to the job and is freed by rs_job_destroy().  Calls on one job are
+ *     serialised internally (a mutex per job); distinct jobs may be used from
+ *     distinct threads.
+ *   - Only odd primes 3 <= p < 2^63 are sieved (the reference's arithmetic
+ *     bound is p < 2^63, kernel_v0.24.6.cu:156-157,197).
+ *   - The factor set is COMPLETE: every (p,k,n) with p prime in [p0,p1],
+ *     n a candidate of k (or, with datless, any n in [nmin,nmax]) and
+ *     p | k*b^n+sign.  The reference reports at most one factor per prime.
+ */
+#ifndef RSIEVE_H
+#define RSIEVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RS_OK 0
+#define RS_ERR_INVALID 1   /* bad argument or malformed ABCD input */
+#define RS_ERR_CUDA 2      /* CUDA runtime error (message has the CUDA text) */
+#define RS_ERR_NOMEM 3     /* host or device allocation failed */
+#define RS_ERR_RANGE 4     /* p range outside 3 <= p < 2^63 */
+#define RS_ERR_NODEVICE 5  /* no CUDA device (the library has no CPU path) */
+#define RS_ERR_CAPACITY 6  /* output buffer too small; *count holds the size needed */
+#define RS_ERR_INTERNAL 7  /* a reported factor failed host re-verification */
+
+typedef struct rs_job rs_job;
+
+/* One removed candidate: p | k*b^n+sign. */
+typedef struct {
+  uint64_t p;
+  uint32_t k;
+  uint32_t n;
+} rs_factor;
+
+/* Controls of the reference CLI (kernel_v0.24.6.cu:705-786), with AUTO = 0. */
+typedef struct {
+  int32_t Q;            /* -Q: subsequence modulus; 0 = chosen by the cost model.
+                           A forced Q is always honoured (the reference only adopts
+                           it when cheaper than Q=1, kernel_v0.24.6.cu:1089-1141). */
+  int32_t hash_m;       /* -m M: at most 2<<M baby steps per prime; 0 = auto. */
+  int32_t block_scale;  /* -b B: primes per launch = 128*2^(B-1) * 128*2^(T-1);   */
+  int32_t thread_scale; /* -t T: 0 = auto (kernel_v0.24.6.cu:817-851).            */
+  int32_t small_prime_scale; /* -s S: accepted for compatibility.  The device sieve
+                           is complete up to sqrt(p1), so S changes nothing. */
+  int32_t datless;      /* -v: report every n in [nmin,nmax] (kernel_v0.24.6.cu:1718-1723) */
+  int32_t host_verify;  /* re-verify every factor on the host with 128-bit
+                           arithmetic (kernel_v0.24.6.cu:1649-1671); default 1 */
+  int32_t device;       /* CUDA device ordinal (the reference hard-codes 0) */
+} rs_options;
+
+/* The plan a job runs with. */
+typedef struct {
+  uint32_t base;
+  int32_t sign;
+  uint32_t num_k;
+  uint32_t num_candidates;
+  uint32_t nmin, nmax;
+  uint32_t Q;            /* subsequence modulus */
+  uint32_t rows;         /* (k, n mod Q) subsequences with candidates */
+  uint32_t x_range;      /* floor(nmax/Q) - floor(nmin/Q) + 1 */
+  uint32_t baby_steps;   /* m */
+  uint32_t giant_steps;  /* T (per row) */
+  uint32_t table_slots;  /* shared-memory hash slots per prime */
+  uint32_t primes_per_launch;
+  double work_per_prime; /* algorithmic montmuls per prime: 2*sqrt(E[R]*X) */
+  uint64_t upload_bytes; /* host->device bytes copied when the job was created */
+} rs_job_info;
+
+/* Counters and device-timed durations of the last rs_sieve_range call. */
+typedef struct {
+  uint64_t primes;       /* primes sieved */
+  uint64_t raw_hits;     /* hash matches that passed the candidate check */
+  uint64_t factors;      /* verified factors */
+  uint64_t p_covered;    /* width of the p-interval covered */
+  double gpu_ms;         /* CUDA-event time from first to last kernel of the call */
+  double bsgs_ms;        /* summed CUDA-event time of the BSGS kernel launches */
+  double sieve_ms;       /* summed time of the prime-sieve kernel launches */
+  double setup_ms;       /* summed time of the per-prime setup kernel launches */
+  uint32_t launches;     /* kernels launched by the call */
+  uint32_t bsgs_launches;
+  uint64_t h2d_bytes;    /* host->device bytes the call copied */
+  uint64_t d2h_bytes;    /* device->host bytes the call copied */
+} rs_stats;
+
+void rs_options_default(rs_options *opt);
+
+/* Parse an ABCD text (kernel_v0.24.6.cu:938-1083), plan the job
+ * (kernel_v0.24.6.cu:1086-1255) and upload it (kernel_v0.24.6.cu:1367-1512). */
+int rs_job_create_abcd(const char *text, size_t len, const rs_options *opt, rs_job **job);
+
+/* Same from arrays: n lists in CSR form (n_offsets[num_k+1]); sign -1 or +1. */
+int rs_job_create(uint32_t base, int32_t sign, uint32_t num_k, const uint32_t *k,
+                  const uint32_t *n_offsets, const uint32_t *n_values, const rs_options *opt,
+                  rs_job **job);
+
+int rs_job_info_get(const rs_job *job, rs_job_info *info);
+
+/* Parse and plan only, no device needed (the reference's planner step,
+ * kernel_v0.24.6.cu:1086-1158, run on the host). */
+int rs_plan_abcd(const char *text, size_t len, const rs_options *opt, rs_job_info *info);
+int rs_job_destroy(rs_job *job);
+
+/* Sieve p in [p0, p1] (inclusive; the reference's while(low < high) loop,
+ * kernel_v0.24.6.cu:1537-1770, without its overshoot past P1).  Factors are
+ * sorted by (p, k, n).  If more than cap are found, returns RS_ERR_CAPACITY
+ * with *count = the number found (none written).  stats may be NULL. */
+int rs_sieve_range(rs_job *job, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
+                   size_t *count, rs_stats *stats);
+
+/* Append factors in the reference's format "%llu | %d*%d^%d-1\n"
+ * (kernel_v0.24.6.cu:1830-1835; "+1" for a Sierpinski job). */
+int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, size_t count);
+
+/* The device prime sieve alone: odd primes in [lo, hi], ascending (replaces the
+ * host generateGPUPrimes, kernel_v0.24.6.cu:1838-1987).  Returns
+ * RS_ERR_CAPACITY with *count = needed when cap is too small. */
+int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *count, int device);
+
+/* Measured throughput of the integer-multiply pipe on this GPU: 32-bit
+ * multiply-class PTX operations per second (the same mix a 64-bit Montgomery
+ * product uses), and 64-bit Montgomery products per second.  No counterpart in
+ * the reference; the roofline of the BSGS kernel is stated against it. */
+int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s);
+
+/* Device arithmetic self-test: n Montgomery products and Jacobi symbols on the
+ * GPU for the given inputs (results written to out_*), used by the parity
+ * tests against the oracle.  a, b < p < 2^63, p odd. */
+int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
+                       uint64_t *out_mulmod, int32_t *out_jacobi_ap, int device);
+
+const char *rs_last_error(void);
+const char *rs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,101 @@
+"""The C ABI library: builds, loads, exports every declared symbol, and its
+host-only logic (ABCD parsing, planning, argument checks) works without a GPU."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "rsieve.h")).read()
+    return sorted(set(re.findall(r"\b(rs_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_exports_match_header(rs):
+    names = _declared()
+    assert set(names) == set(rs.EXPORTS)
+    lib = ctypes.CDLL(rs.LIB)
+    for n in names:
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", rs.LIB], capture_output=True, text=True).stdout
+    for n in names:
+        assert re.search(r"\bT " + n + r"\b", out), n
+
+
+def test_version(rs):
+    assert "sm_103a" in rs.version()
+
+
+def test_plan_sr745(rs, sr745_text):
+    info = rs.plan_abcd(sr745_text)
+    assert info["base"] == 745 and info["sign"] == -1
+    assert info["num_k"] == 22 and info["num_candidates"] == 65111
+    assert info["nmin"] == 182644 and info["nmax"] == 250000
+    # the plan covers the whole x range: m*T >= X
+    assert info["baby_steps"] * info["giant_steps"] >= info["x_range"]
+    assert info["table_slots"] >= 2 * info["baby_steps"]
+    forced = rs.plan_abcd(sr745_text, Q=18)
+    assert forced["Q"] == 18 and forced["rows"] == 198 and forced["x_range"] == 3743
+
+
+def test_plan_forced_m(rs, sr745_text):
+    info = rs.plan_abcd(sr745_text, hash_m=6, Q=2)
+    assert info["baby_steps"] <= 2 << 6
+    assert info["baby_steps"] * info["giant_steps"] >= info["x_range"]
+
+
+def test_plan_datless_rows(rs):
+    txt = "ABCD 5*3^$a-1 [100]\n6\n6\n"
+    assert rs.plan_abcd(txt, Q=6)["rows"] == 1
+    assert rs.plan_abcd(txt, Q=6, datless=1)["rows"] == 6
+
+
+@pytest.mark.parametrize("bad", [
+    "12\n",
+    "ABCD 3*2^$a-1 [10]\n0\n",
+    "ABCD 3*2^$a-1 [10]\nABCD 5*3^$a-1 [10]\n",
+    "ABCD 3*2^$a-1 [10]\nABCD 5*2^$a+1 [10]\n",
+    "ABCD x*2^$a-1 [10]\n",
+    "ABCD 3*2^$a-1 10\n",
+    "",
+])
+def test_plan_rejects_malformed(rs, bad):
+    with pytest.raises(rs.RsieveError) as e:
+        rs.plan_abcd(bad)
+    assert e.value.code == rs.RS_ERR_INVALID
+
+
+def test_plan_sierpinski_and_crlf(rs):
+    info = rs.plan_abcd("ABCD 7*2^$a+1 [10]\r\n2\r\n\r\n3\r\n")
+    assert info["sign"] == 1 and info["num_candidates"] == 3 and info["nmax"] == 15
+
+
+def test_no_cpu_fallback(rs):
+    """Without a GPU the library refuses work instead of computing on the CPU."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("GPU present")
+    except ImportError:
+        pass
+    with pytest.raises(rs.RsieveError) as e:
+        rs.Job("ABCD 3*2^$a-1 [10]\n2\n")
+    assert e.value.code == rs.RS_ERR_NODEVICE
+    with pytest.raises(rs.RsieveError):
+        rs.gpu_primes(3, 1000)
+
+
+def test_cli_help(rs):
+    out = subprocess.run([rs.CLI, "-h"], capture_output=True, text=True)
+    assert out.returncode == 0 and "-Q Q" in out.stdout
+
+
+def test_cli_rejects_odd_q(rs, tmp_path):
+    out = subprocess.run([rs.CLI, "-Q", "3"], capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode == 1 and "Q must be an even integer" in out.stdout

@@ -1,0 +1,176 @@
+"""Parity of the CUDA path with the CPU oracle (run on the GB300 machine).
+
+Bit-exact factor sets: the GPU reports every (p,k,n) the oracle reports and
+nothing else, on seeded synthetic jobs, on the reference's own sr_745.abcd,
+and on edge cases (Sierpinski, even k, base 2, p dividing b or k, tiny p,
+x range starting at 0, forced Q/m, datless).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _set(f):
+    return [(int(a), int(b), int(c)) for a, b, c in f]
+
+
+def _both(rs, oracle_mod, base, sign, ks, nlists, p0, p1, datless=False, **opts):
+    job = rs.Job(base=base, sign=sign, ks=ks, nlists=nlists, datless=int(datless), **opts)
+    g, st = job.sieve(p0, p1)
+    oj = oracle_mod.Job.from_arrays(base, sign, ks, [np.asarray(x) for x in nlists])
+    o, npr = oj.sieve(p0, p1, datless=datless)
+    job.close()
+    assert st["primes"] == npr
+    return _set(g), _set(o), st
+
+
+def test_arith_montmul_and_jacobi(rs, oracle_mod):
+    rng = np.random.default_rng(11)
+    ps = oracle_mod.primes(10**13, 10**13 + 3000).tolist()
+    ps += oracle_mod.primes(2**62 - 200000, 2**62).tolist()
+    ps += oracle_mod.primes(2**63 - 20000, 2**63 - 1).tolist()
+    ps += [3, 5, 7, 2**31 - 1, 4294967311]
+    a, b, p = [], [], []
+    for P in ps:
+        for _ in range(4):
+            a.append(int(rng.integers(0, P)) if P > 2 else 1)
+            b.append(int(rng.integers(0, P)))
+            p.append(P)
+        a += [P - 1, 0, 1 % P, (1 << 32) % P]
+        b += [P - 1, P - 1, P - 1, (1 << 32) % P]
+        p += [P, P, P, P]
+    mm, jj = rs.arith_check(a, b, p)
+    for i in range(len(a)):
+        assert int(mm[i]) == a[i] * b[i] % p[i], (a[i], b[i], p[i])
+        k = a[i] & 0xFFFFFFFF
+        assert int(jj[i]) == oracle_mod.jacobi(k, p[i]), (k, p[i])
+
+
+@pytest.mark.parametrize("lo,hi", [
+    (3, 200000), (10**9, 10**9 + 3 * 10**6), (10**13 - 10**6, 10**13 + 10**6),
+    (2**50, 2**50 + 10**6), (2**62 - 10**6, 2**62 + 10**6), (2**63 - 10**6, 2**63 - 1),
+    (101, 101), (100, 103), (2**32 - 50, 2**32 + 50),
+])
+def test_gpu_primes_match_oracle(rs, oracle_mod, lo, hi):
+    g = rs.gpu_primes(lo, hi)
+    o = oracle_mod.primes(lo, hi)
+    assert np.array_equal(g, o)
+
+
+def test_plain_small_full(rs, oracle_mod):
+    """The small plain workload in full: b=745, 22 k, p in [1e9, 1.02e9)."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    p0, p1 = S.PLAIN_SMALL_RANGE
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p1)
+    assert len(o) > 0
+    assert g == o
+
+
+def test_plain_steady_subwindow(rs, oracle_mod):
+    """A 2e7-wide sub-window of the steady-state workload at 1e13."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**13, 10**13 + 2 * 10**7)
+    assert g == o
+
+
+@pytest.mark.parametrize("opts", [{}, {"Q": 18}, {"Q": 2}, {"Q": 18, "hash_m": 5}, {"Q": 6, "hash_m": 9}])
+def test_sr745_vs_oracle(rs, oracle_mod, sr745_text, opts):
+    """The reference's own test file (datless, so hits exist at small p)."""
+    job = rs.Job(sr745_text, datless=1, **opts)
+    g, st = job.sieve(10**6, 10**6 + 4 * 10**6)
+    oj = oracle_mod.Job.from_abcd(sr745_text)
+    o, npr = oj.sieve(10**6, 10**6 + 4 * 10**6, datless=True)
+    job.close()
+    assert st["primes"] == npr
+    assert _set(g) == _set(o)
+    assert len(o) > 100
+
+
+def test_sr745_negative_kat(rs, sr745_text, kat):
+    """Sieved to 5e12 (sr_745.abcd:1): no candidate has a factor below it."""
+    lim = kat["negative"]["sieved_to"]
+    job = rs.Job(sr745_text)
+    g, st = job.sieve(lim - 2 * 10**8, lim)
+    assert len(g) == 0 and st["primes"] > 6 * 10**6
+    g, st = job.sieve(10**9, 10**9 + 10**8)
+    assert len(g) == 0
+
+
+def test_sr745_datless_kat(rs, sr745_text, kat):
+    """102297149781479 | 18300*745^242670-1 (kernel_v0.24.6.cu:244); n is not a candidate."""
+    d = kat["datless"]
+    lo = kat["default_range"]["low"]
+    for Q in (0, 18):
+        job = rs.Job(sr745_text, datless=1, Q=Q)
+        g, st = job.sieve(lo, lo + kat["default_range"]["width_per_scale"])
+        assert (d["p"], d["k"], d["n"]) in _set(g)
+        job.close()
+    job = rs.Job(sr745_text)
+    g, st = job.sieve(d["p"] - 10**5, d["p"] + 10**5)
+    assert (d["p"], d["k"], d["n"]) not in _set(g)
+
+
+@pytest.mark.parametrize("case", [
+    # base, sign, ks, n range, density, p0, p1, opts
+    (2, -1, [3, 5, 7, 9, 15, 27], (1000, 3000), 0.3, 10**7, 10**7 + 10**6, {}),
+    (2, 1, [3, 5, 7, 9, 15, 27], (1000, 3000), 0.3, 10**7, 10**7 + 10**6, {}),
+    (10, -1, [4, 12, 48, 96, 1024], (50, 900), 0.5, 3, 300000, {}),
+    (3, -1, [2, 4, 8, 16], (1, 40), 1.0, 3, 100000, {"Q": 6}),
+    (745, -1, [18300, 1160], (5, 20), 1.0, 3, 50000, {"Q": 18}),
+    (6, 1, [1, 35, 77], (100, 20000), 0.1, 10**9, 10**9 + 10**6, {"Q": 3}),
+    (1024, -1, [3, 7, 11], (5000, 60000), 0.05, 10**12, 10**12 + 10**6, {}),
+])
+def test_edge_cases(rs, oracle_mod, case):
+    base, sign, ks, (nlo, nhi), dens, p0, p1, opts = case
+    rng = np.random.default_rng(abs(hash((base, sign, nlo))) % 2**32)
+    nlists = []
+    for _ in ks:
+        ns = np.arange(nlo, nhi + 1)
+        keep = ns[rng.random(ns.size) < dens]
+        if keep.size == 0:
+            keep = ns[:1]
+        nlists.append(keep.astype(np.uint32))
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, base, sign, ks, nlists, p0, p1, datless=datless, **opts)
+        assert g == o, (case, datless, len(g), len(o))
+
+
+def test_range_additivity_and_boundaries(rs, oracle_mod):
+    """[a,c] == [a,b] + [b+1,c]; primes exactly at p0 and p1 are included."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(2)
+    job = rs.Job(base=b, sign=s, ks=ks, nlists=nl, datless=1)
+    a, c = 10**9, 10**9 + 4 * 10**6
+    full, _ = job.sieve(a, c)
+    mid = a + 1234567
+    left, _ = job.sieve(a, mid)
+    right, _ = job.sieve(mid + 1, c)
+    assert _set(full) == _set(left) + _set(right)
+    ps = sorted({x[0] for x in _set(full)})
+    assert ps, "datless window should have hits"
+    p = ps[len(ps) // 2]
+    at, _ = job.sieve(p, p)
+    assert {x[0] for x in _set(at)} == {p}
+    job.close()
+
+
+def test_every_factor_verifies_at_scale(rs, oracle_mod):
+    """A 1e10-wide slice of the steady-state workload: every factor passes an
+    independent modexp check (size-independent property)."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    job = rs.Job(base=b, sign=s, ks=ks, nlists=nl)
+    g, st = job.sieve(10**13, 10**13 + 10**10)
+    cand = {(int(k), int(n)) for k, ns in zip(ks, nl) for n in ns}
+    for p, k, n in _set(g):
+        assert oracle_mod.verify(p, k, b, n, s)
+        assert (k, n) in cand
+    assert st["primes"] > 3 * 10**8
+    job.close()
