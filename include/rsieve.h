@@ -94,6 +94,7 @@ typedef struct {
   double bsgs_ms;        /* summed CUDA-event time of the BSGS kernel launches */
   double sieve_ms;       /* summed time of the prime-sieve kernel launches */
   double setup_ms;       /* summed time of the per-prime setup kernel launches */
+  double exact_ms;       /* summed time of the exact-path BSGS launches (rare primes) */
   uint32_t launches;     /* kernels launched by the call */
   uint32_t bsgs_launches;
   uint64_t h2d_bytes;    /* host->device bytes the call copied */
@@ -134,11 +135,12 @@ int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, si
  * RS_ERR_CAPACITY with *count = needed when cap is too small. */
 int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *count, int device);
 
-/* Measured throughput of the integer-multiply pipe on this GPU: 32-bit
- * multiply-class PTX operations per second (the same mix a 64-bit Montgomery
- * product uses), and 64-bit Montgomery products per second.  No counterpart in
- * the reference; the roofline of the BSGS kernel is stated against it. */
-int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s);
+/* Measured throughput of the integer-multiply pipe on this GPU: plain 32-bit
+ * mad.lo operations per second, and 64-bit modular products per second in the
+ * two forms the kernels use (Montgomery, and Shoup's product by a fixed
+ * multiplier), each from independent dependency chains.  No counterpart in the
+ * reference; the roofline of the BSGS kernel is stated against it. */
+int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
 
 /* Device arithmetic self-test: n Montgomery products and Jacobi symbols on the
  * GPU for the given inputs (results written to out_*), used by the parity
