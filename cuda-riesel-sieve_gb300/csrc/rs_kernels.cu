@@ -412,10 +412,10 @@ struct __align__(16) Match {
   uint32_t s;     // giant index
 };
 
-// 16-bit tag of a residue: bits [tl, tl+16) above the bucket index, never 0
-// (0 marks an empty slot).
+// 16-bit tag of a residue: bits [tl, tl+16) of its low word, above the
+// bucket index (tl <= 16), never 0 (0 marks an empty slot).
 __device__ __forceinline__ uint32_t tag16(uint64_t v, uint32_t tl) {
-  return max((uint32_t)(v >> tl) & 0xffffu, 1u);
+  return max(((uint32_t)v >> tl) & 0xffffu, 1u);
 }
 
 // True iff one of the 8 tags of bucket q equals the tag pair T = t*0x10001.
@@ -424,33 +424,92 @@ __device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
   return (m & 0xffffu) == 0 || (m >> 16) == 0;
 }
 
+// Hash-table view of one warp's shared memory.
+struct WarpTable {
+  uint4 *tab4;
+  uint16_t *tab16;
+  uint32_t *cnt;
+  uint32_t bmask, tl;
+
+  __device__ __forceinline__ void insert(uint64_t v) const {
+    uint32_t b = (uint32_t)v & bmask;
+    uint32_t c = atomicAdd(&cnt[b], 1u);
+#pragma unroll 1
+    for (uint32_t g = 0; c >= (uint32_t)kBucket && g <= bmask; g++) {
+      b = (b + 1) & bmask;
+      c = atomicAdd(&cnt[b], 1u);
+    }
+    if (c < (uint32_t)kBucket) tab16[b * kBucket + c] = (uint16_t)tag16(v, tl);
+  }
+
+  // True iff some entry with the tag of y lies in y's probe sequence.
+  __device__ __forceinline__ bool probe(uint64_t y) const {
+    uint32_t b = (uint32_t)y & bmask;
+    const uint32_t T = tag16(y, tl) * 0x10001u;
+    bool hit = false;
+#pragma unroll 1
+    for (uint32_t g = 0; g <= bmask; g++) {
+      const uint4 q = tab4[b];
+      hit |= bucket_has(q, T);
+      if (q.w < 0x10000u) break;  // slot 7 empty: not full, the probe ends here
+      b = (b + 1) & bmask;
+    }
+    return hit;
+  }
+};
+
+struct MatchList {
+  Match *list;
+  uint32_t *count;
+  __device__ __forceinline__ void push(uint64_t y, uint32_t slot, uint32_t s) const {
+    const uint32_t idx = atomicAdd(count, 1u);
+    if (idx < (uint32_t)kMatchCap) {
+      Match mt;
+      mt.y = y;
+      mt.slot = slot;
+      mt.s = s;
+      list[idx] = mt;
+    }
+  }
+};
+
 // Per-warp shared memory of the fast kernel:
 //   [NB buckets x 16 B][NB counters x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
 // Buckets fill slot 0..7 in order (a per-bucket atomic counter hands out slots),
 // so a bucket is full iff its slot 7 is nonzero, and an entry overflows into
 // bucket b+1 only when bucket b is full: a probe scans from the home bucket to
 // the first bucket that is not full.
+//
+// Each lane runs two independent product chains in both phases (baby steps
+// j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
+// time) so that consecutive dependent Shoup products overlap.
+// TL = giant steps handled side by side per row (min(T, 32)).
+template <int TL>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
+  constexpr uint32_t RPI = 32 / TL;  // row slots per lane-group pass
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t NB = 1u << J.table_log2;
-  const uint32_t bmask = NB - 1;
-  const uint32_t tl = J.table_log2;
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * J.warp_smem;
-  uint4 *tab4 = reinterpret_cast<uint4 *>(base);
-  uint16_t *tab16 = reinterpret_cast<uint16_t *>(base);
-  uint32_t *cnt = reinterpret_cast<uint32_t *>(base + NB * 16);
+  WarpTable W;
+  W.tab4 = reinterpret_cast<uint4 *>(base);
+  W.tab16 = reinterpret_cast<uint16_t *>(base);
+  W.cnt = reinterpret_cast<uint32_t *>(base + NB * 16);
+  W.bmask = NB - 1;
+  W.tl = J.table_log2;
   uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
-  Match *mlist = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
-  uint32_t *mcount = reinterpret_cast<uint32_t *>(mlist + kMatchCap);
-  const uint32_t lane_t = lane & (J.tlanes - 1);
-  const uint32_t lane_row = lane / J.tlanes;
+  MatchList ML;
+  ML.list = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
+  ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
+  const uint32_t lane_t = lane & (TL - 1);
+  const uint32_t lane_row = lane / TL;
   const uint32_t total = *cb.count;
   const uint32_t n = total < cb.cap ? total : cb.cap;
   const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
   const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
-  const uint32_t nbaby = (J.m + 31) / 32;
+  const uint32_t nbaby2 = (J.m + 63) / 64;  // iterations of the two-chain baby loop
+  const uint32_t spl = J.steps_per_lane;
 
   if (first < n) stage_copy(stage0, J, cb, first, J.stage_elems, lane);
   else stage_commit_empty();
@@ -471,108 +530,106 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       // Multipliers in normal form with their Shoup constants; the values
       // they multiply stay in Montgomery form, so products stay comparable.
       const uint64_t Bm = cur[kElBs], Gm = cur[kElGs];
+      const uint64_t B2m = montmul(Bm, Bm, p, pinv);  // B^64
       const uint64_t Bw = montmul(Bm, 1, p, pinv), Bq = shoup_const(Bm, pinv);
+      const uint64_t B2w = montmul(B2m, 1, p, pinv), B2q = shoup_const(B2m, pinv);
       const uint64_t Gw = montmul(Gm, 1, p, pinv), Gq = shoup_const(Gm, pinv);
       const uint64_t Glm = cur[kElG + lane];
       const uint64_t Glw = montmul(Glm, 1, p, pinv), Glq = shoup_const(Glm, pinv);
       const uint64_t Bl = cur[kElB + lane];
+      const uint64_t Bl32 = shoup_mul(Bl, Bw, Bq, p);  // B^(lane+32)
       // clear the table and the bucket counters
       const uint4 z4 = make_uint4(0, 0, 0, 0);
-      for (uint32_t q = lane; q < NB + NB / 4; q += 32) tab4[q] = z4;
-      if (lane == 0) *mcount = 0;
+      for (uint32_t q = lane; q < NB + NB / 4; q += 32) W.tab4[q] = z4;
+      if (lane == 0) *ML.count = 0;
       __syncwarp();
 
-      // Baby steps: lane owns j = lane + 32*t.
-      uint64_t v = Bl;
+      // Baby steps: chain A owns j = lane + 64t, chain B j = lane + 32 + 64t.
+      {
+        uint64_t va = Bl, vb = Bl32;
 #pragma unroll 1
-      for (uint32_t t = 0; t < nbaby; t++) {
-        if (lane + 32 * t < J.m) {
-          uint32_t b = (uint32_t)v & bmask;
-          uint32_t c = atomicAdd(&cnt[b], 1u);
-#pragma unroll 1
-          for (uint32_t g = 0; c >= (uint32_t)kBucket && g < NB; g++) {
-            b = (b + 1) & bmask;
-            c = atomicAdd(&cnt[b], 1u);
-          }
-          if (c < (uint32_t)kBucket) tab16[b * kBucket + c] = (uint16_t)tag16(v, tl);
+        for (uint32_t t = 0; t < nbaby2; t++) {
+          const uint32_t ja = lane + 64 * t;
+          if (ja < J.m) W.insert(va);
+          if (ja + 32 < J.m) W.insert(vb);
+          va = shoup_mul(va, B2w, B2q, p);
+          vb = shoup_mul(vb, B2w, B2q, p);
         }
-        v = shoup_mul(v, Bw, Bq, p);
       }
       __syncwarp();
 
-      // Giant steps: lane (lane_row, lane_t) takes slot gi*rows_per_it + lane_row and
-      // giant indices s = lane_t + 1 (+32 per extra step).
-      const uint32_t ngi = (nact + J.rows_per_it - 1) / J.rows_per_it;
+      // Giant steps: lane (lane_row, lane_t) takes row slots g*RPI + lane_row for
+      // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
+      const uint32_t ngi = (nact + RPI - 1) / RPI;
 #pragma unroll 1
-      for (uint32_t gi = 0; gi < ngi; gi++) {
-        const uint32_t slot = gi * J.rows_per_it + lane_row;
-        const bool active = slot < nact;
-        const uint32_t sl = active ? slot : 0;
-        const uint64_t Vs = J.stage_full ? cur[kElV + sl] : rec_el(J, cb, kElV + sl, i);
-        uint64_t y = shoup_mul(Vs, Glw, Glq, p);
+      for (uint32_t gi = 0; gi < ngi; gi += 2) {
+        const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
+        const bool aa = sa < nact, ab = sb < nact;
+        const uint64_t Va = J.stage_full ? cur[kElV + (aa ? sa : 0)] : rec_el(J, cb, kElV + (aa ? sa : 0), i);
+        const uint64_t Vb = J.stage_full ? cur[kElV + (ab ? sb : 0)] : rec_el(J, cb, kElV + (ab ? sb : 0), i);
+        uint64_t ya = shoup_mul(Va, Glw, Glq, p);
+        uint64_t yb = shoup_mul(Vb, Glw, Glq, p);
         uint32_t s = lane_t + 1;
 #pragma unroll 1
-        for (uint32_t u = 0; u < J.steps_per_lane; u++) {
-          if (active) {
-            uint32_t b = (uint32_t)y & bmask;
-            const uint32_t T = tag16(y, tl) * 0x10001u;
-            bool hit = false;
-#pragma unroll 1
-            for (uint32_t g = 0; g < NB; g++) {
-              const uint4 q = tab4[b];
-              hit |= bucket_has(q, T);
-              if (q.w < 0x10000u) break;  // slot 7 empty: not full, the probe ends here
-              b = (b + 1) & bmask;
-            }
-            if (hit) {
-              const uint32_t idx = atomicAdd(mcount, 1u);
-              if (idx < (uint32_t)kMatchCap) {
-                Match mt;
-                mt.y = y;
-                mt.slot = slot;
-                mt.s = s;
-                mlist[idx] = mt;
-              }
-            }
-          }
-          if (u + 1 < J.steps_per_lane) {
-            y = shoup_mul(y, Gw, Gq, p);
-            s += 32;
-          }
+        for (uint32_t u = 0;; u++) {
+          if (aa && W.probe(ya)) ML.push(ya, sa, s);
+          if (ab && W.probe(yb)) ML.push(yb, sb, s);
+          if (u + 1 >= spl) break;
+          ya = shoup_mul(ya, Gw, Gq, p);
+          yb = shoup_mul(yb, Gw, Gq, p);
+          s += 32;
         }
       }
       __syncwarp();
 
       // Tag matches: recompute the baby steps and compare full 64-bit values.
-      const uint32_t mc = *mcount;
+      const uint32_t mc = *ML.count;
       if (mc > (uint32_t)kMatchCap) {
         if (lane == 0) {
           const uint32_t r = atomicAdd(cb.redo_count, 1u);
           if (r < cb.cap) cb.redo[r] = i;
         }
       } else if (mc > 0) {
-        v = Bl;
+        uint64_t va = Bl, vb = Bl32;
 #pragma unroll 1
-        for (uint32_t t = 0; t < nbaby; t++) {
-          const uint32_t j = lane + 32 * t;
-          if (j < J.m) {
+        for (uint32_t t = 0; t < nbaby2; t++) {
 #pragma unroll 1
-            for (uint32_t q = 0; q < mc; q++) {
-              const Match mt = mlist[q];
-              if (mt.y == v) {
-                const uint64_t pk = J.stage_full ? cur[J.el_row + (mt.slot >> 2)]
-                                                 : rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
-                record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s, j);
+          for (uint32_t h = 0; h < 2; h++) {
+            const uint32_t j = lane + 64 * t + 32 * h;
+            const uint64_t v = h ? vb : va;
+            if (j < J.m) {
+#pragma unroll 1
+              for (uint32_t q = 0; q < mc; q++) {
+                const Match mt = ML.list[q];
+                if (mt.y == v) {
+                  const uint64_t pk = J.stage_full ? cur[J.el_row + (mt.slot >> 2)]
+                                                   : rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                  record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s, j);
+                }
               }
             }
           }
-          v = shoup_mul(v, Bw, Bq, p);
+          va = shoup_mul(va, B2w, B2q, p);
+          vb = shoup_mul(vb, B2w, B2q, p);
         }
       }
     }
     __syncwarp();
   }
   stage_wait_all();
+}
+
+typedef void (*BsgsFn)(JobDev, ChunkBufs, HitBufs);
+
+static BsgsFn bsgs_fn(uint32_t tlanes) {
+  switch (tlanes) {
+    case 1: return bsgs_kernel<1>;
+    case 2: return bsgs_kernel<2>;
+    case 4: return bsgs_kernel<4>;
+    case 8: return bsgs_kernel<8>;
+    case 16: return bsgs_kernel<16>;
+    default: return bsgs_kernel<32>;
+  }
 }
 
 int bsgs_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (int)job.warp_smem; }
@@ -666,14 +723,14 @@ static cudaError_t configure_one(const void *fn, int smem, int device, int *grid
 }
 
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out) {
-  cudaError_t e = configure_one((const void *)bsgs_kernel, bsgs_smem_bytes(job), device, grid_out);
+  cudaError_t e = configure_one((const void *)bsgs_fn(job.tlanes), bsgs_smem_bytes(job), device, grid_out);
   if (e != cudaSuccess) return e;
   return configure_one((const void *)bsgs_exact_kernel, bsgs_exact_smem_bytes(job), device, exact_grid_out);
 }
 
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st) {
-  bsgs_kernel<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+  bsgs_fn(job.tlanes)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();
 }
 
