@@ -53,6 +53,18 @@ WORKLOAD = ("plain_steady: b=745, 22 seeded odd k in [3,1e6], n in [180000,25000
             "all primes p in [1e13, 1e13+1e11)")
 
 
+def bsgs_bytes_per_prime():
+    """DRAM bytes per prime of the BSGS kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "bsgs_kernel.plain_steady.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_prime:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -289,6 +301,8 @@ def main() -> None:
     alg_ops = primes * info["work_per_prime"] * MONTMUL_MULS
     achieved = alg_ops / (bsgs_ms / 1e3) / 1e12
     peak = modmul_per_s * MONTMUL_MULS / 1e12
+    bpp = bsgs_bytes_per_prime()
+    traffic = None if bpp is None or not bsgs_launches else bpp * primes / bsgs_launches
 
     e2e = None
     if not args.no_e2e:
@@ -328,7 +342,8 @@ def main() -> None:
         },
         "roofline": {
             "bound": "imad", "achieved": achieved, "peak": peak, "unit": "Tops/s", "frac": achieved / peak,
-            "traffic": None,
+            "traffic": traffic,
+            "traffic_unit": "DRAM bytes per BSGS launch (ncu dram__bytes_read+write per prime x primes per launch)",
             "what": ("32-bit multiply-class ops of the algorithmic BSGS work (2*sqrt(E[R]*X) Montgomery "
                      f"products per prime = {info['work_per_prime']:.0f}, x{MONTMUL_MULS} ops) per second of "
                      "BSGS kernel time"),
