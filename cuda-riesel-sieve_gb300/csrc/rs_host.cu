@@ -38,6 +38,16 @@ static int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+int rs::set_error(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
 #define CUDA_TRY(expr)                                                                   \
   do {                                                                                   \
     cudaError_t _e = (expr);                                                             \

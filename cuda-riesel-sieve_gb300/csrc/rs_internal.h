@@ -116,6 +116,9 @@ cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *ex
 
 cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
                                  uint32_t total_words, uint32_t *bits, cudaStream_t st);
+// Record an error for rs_last_error() and return code (rs_host.cu).
+int set_error(int code, const char *fmt, ...);
+
 cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
 cudaError_t run_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
                             uint64_t *out_mm, int32_t *out_j);

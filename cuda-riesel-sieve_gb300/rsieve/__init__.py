@@ -28,7 +28,7 @@ FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u4"), ("n", "<u4")])
 EXPORTS = (
     "rs_options_default", "rs_job_create_abcd", "rs_job_create", "rs_job_info_get",
     "rs_plan_abcd", "rs_job_destroy", "rs_sieve_range", "rs_write_factors", "rs_gpu_primes",
-    "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version",
+    "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
 )
 
 
@@ -119,6 +119,7 @@ def lib():
         L.rs_bench_imad.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_double)]
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
+        L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
         L.rs_last_error.restype = ctypes.c_char_p
         L.rs_version.restype = ctypes.c_char_p
         _lib = L

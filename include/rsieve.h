@@ -135,6 +135,31 @@ int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, si
  * RS_ERR_CAPACITY with *count = needed when cap is too small. */
 int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *count, int device);
 
+/* The device prime sieve for callers that cannot allocate device memory (no
+ * counterpart in the reference).  Code that runs under a device-memory budget or
+ * pool that forbids new allocations, a plug-in whose host owns all device memory,
+ * or a caller recording work for a CUDA graph cannot call cudaMalloc at this
+ * point; this entry point allocates nothing.  The caller passes every buffer as
+ * device memory it owns:
+ *   sieve_primes  every odd prime up to sqrt(hi), ascending (best: the
+ *                 consecutive odd primes 3, 5, 7, ...), n_sieve of them
+ *   sieve_rcp     floor(2^64 / sieve_primes[i]) for each of them
+ *   out, cap      the odd primes of [lo, hi], in no particular order
+ *   count         the number found (may exceed cap; then only cap are written)
+ * The one scratch buffer, the window's large-prime bitmap, is a fixed 4 MB array
+ * in the library's device image that every GPU loading the library holds until
+ * the process exits.  It limits a call to windows of at most 2^25 odd numbers
+ * (hi - lo < about 6.7e7); wider windows return RS_ERR_RANGE, so split the range.
+ * All calls share that array and every call clears it first: calls whose work
+ * overlaps on the GPU (different streams, or threads sharing a device) race on it
+ * and must be serialised by the caller.  The call is asynchronous on `stream`
+ * (a cudaStream_t; NULL for the legacy default stream) on the current device;
+ * results are valid once the stream has reached this point.  The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture. */
+int rs_gpu_primes_static(uint64_t lo, uint64_t hi, const uint32_t *sieve_primes, const uint64_t *sieve_rcp,
+                         uint32_t n_sieve, uint64_t *out, uint32_t cap, uint32_t *count, void *stream);
+
 /* Measured throughput of the integer-multiply pipe on this GPU: plain 32-bit
  * mad.lo operations per second, and 64-bit modular products per second in the
  * two forms the kernels use (Montgomery, and Shoup's product by a fixed
