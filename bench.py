@@ -240,6 +240,8 @@ def main() -> None:
     ap.add_argument("--slice", type=float, default=SLICE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--Q", type=int, default=0, help="force the subsequence modulus (default: planner)")
+    ap.add_argument("--hash-m", type=int, default=0, help="cap baby steps at 2<<M (default: planner)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -263,7 +265,7 @@ def main() -> None:
     mul_ops, mont_per_s, shoup_per_s = rsieve.bench_imad(dev)
     modmul_per_s = max(mont_per_s, shoup_per_s)
 
-    job = rsieve.Job(base=b, sign=s, ks=ks, nlists=nl, device=dev)
+    job = rsieve.Job(base=b, sign=s, ks=ks, nlists=nl, device=dev, Q=args.Q, hash_m=args.hash_m)
     info = job.info
     # warm-up: slices just below the window
     for w in range(args.warmup):
@@ -313,7 +315,7 @@ def main() -> None:
         for step in range(e2e_steps):
             idx = step * world + rank
             a = P_START + idx * slice_w
-            with rsieve.Job(abcd, device=dev) as j2:
+            with rsieve.Job(abcd, device=dev, Q=args.Q, hash_m=args.hash_m) as j2:
                 f, st = j2.sieve(a, a + slice_w - 1)
                 h2d += j2.info["upload_bytes"] + st["h2d_bytes"]
                 d2h += st["d2h_bytes"]

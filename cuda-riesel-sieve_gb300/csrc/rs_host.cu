@@ -242,9 +242,11 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
       const uint32_t tlanes = (uint32_t)std::min<uint64_t>(T, 32);
       const uint32_t rpi = 32 / tlanes;
       const uint32_t spl = (uint32_t)std::max<uint64_t>(1, T / 32);
+      // Per-lane units of one baby or giant step (a Shoup product plus a table
+      // operation, about equal on GB300), the table clear, and the per-prime
+      // setup kernel, whose measured cost grows with the number of rows.
       double cost = std::ceil((double)m / 32.0) + std::ceil(ER / rpi) * spl +
-                    (double)(1u << slog) / 1024.0 +
-                    (K * (2.0 + Q / 2.0) + ER + 63.0 + 40.0) / 32.0;
+                    (double)(1u << slog) / 1024.0 + 3.7 + 0.062 * rows;
       if (cost < best) {
         best = cost;
         pl.Q = Q;

@@ -183,7 +183,7 @@ __device__ __forceinline__ void rec_st2(uint64_t *rec, uint32_t e, uint64_t a, u
   *reinterpret_cast<uint4 *>(rec + e) = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
 }
 
-constexpr uint32_t kSetupRegQ = 8;  // Q up to this keeps the table of b^r*B^e0 in registers
+constexpr uint32_t kSetupRegQ = 8;  // Q up to this keeps the table of b^r*B^e0 in shared memory
 
 __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -242,20 +242,16 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
 
   // HB[r] = b^r * B^e0 (Montgomery form) with the Shoup constant of HB[r] taken
   // as an integer, so the start value of row (k, r) is the single product k*HB[r].
-  uint64_t HB[kSetupRegQ], HBq[kSetupRegQ];
+  // Kept per thread in shared memory (indexed by r without a select chain).
+  __shared__ uint64_t hb_sm[kSetupRegQ][2][128];
   const bool regtab = J.Q <= kSetupRegQ;
   if (regtab) {
     uint64_t h = H;
-#pragma unroll
-    for (uint32_t r = 0; r < kSetupRegQ; r++) {
-      if (r < J.Q) {
-        HB[r] = h;
-        HBq[r] = shoup_const(montmul(h, r2, M), M.pinv);
-        h = shoup_mul(h, bmod, bq, p);
-      } else {
-        HB[r] = 0;
-        HBq[r] = 0;
-      }
+#pragma unroll 1
+    for (uint32_t r = 0; r < J.Q; r++) {
+      hb_sm[r][0][threadIdx.x] = h;
+      hb_sm[r][1][threadIdx.x] = shoup_const(montmul(h, r2, M), M.pinv);
+      h = shoup_mul(h, bmod, bq, p);
     }
   }
 
@@ -294,14 +290,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
         const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
         if (!act) continue;
         if (regtab) {
-          uint64_t w = HB[0], wq = HBq[0];
-#pragma unroll
-          for (uint32_t t = 1; t < kSetupRegQ; t++)
-            if (r == t) {
-              w = HB[t];
-              wq = HBq[t];
-            }
-          V = shoup_mul(kx, w, wq, p);
+          V = shoup_mul(kx, hb_sm[r][0][threadIdx.x], hb_sm[r][1][threadIdx.x], p);
         } else {
           if (!have) {
             V = montmul(montmul(kx, r2, M), H, M);
