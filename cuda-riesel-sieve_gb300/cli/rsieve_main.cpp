@@ -32,6 +32,10 @@ static void usage() {
   printf("-t SCALE : (see -b).\n");
   printf("-s SCALE : Accepted for compatibility; the device sieve is always complete.\n");
   printf("-v       : Don't verify: report every n in [nmin,nmax] (datless).\n");
+  printf("-w FILE  : After sieving, write FILE: the input ABCD without the candidates whose\n");
+  printf("           factors are in the factor file, headers marked \"// Sieved to P1\".\n");
+  printf("-C FILE  : Checkpoint: resume from the p recorded in FILE (if it is for the same\n");
+  printf("           input and P1) and record progress there after every block of launches.\n");
   printf("-h       : Prints this help\n");
 }
 
@@ -44,7 +48,8 @@ int main(int argc, char **argv) {
   int block_scale = 1, thread_scale = 1;
   bool scale_given = false;
   int inp;
-  while ((inp = getopt(argc, argv, "b:hi:m:p:P:Q:O:s:t:v")) != -1) {
+  const char *abcd_out = nullptr, *ckpt = nullptr;
+  while ((inp = getopt(argc, argv, "b:hi:m:p:P:Q:O:s:t:vw:C:")) != -1) {
     switch (inp) {
       case 'b': block_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
       case 't': thread_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
@@ -65,6 +70,8 @@ int main(int argc, char **argv) {
       case 'O': factor_file = optarg; break;
       case 's': opt.small_prime_scale = (int)strtol(optarg, nullptr, 0); break;
       case 'v': opt.datless = 1; opt.host_verify = 1; break;
+      case 'w': abcd_out = optarg; break;
+      case 'C': ckpt = optarg; break;
       default: return 0;
     }
   }
@@ -117,9 +124,40 @@ int main(int argc, char **argv) {
          info.Q, info.rows, info.x_range, info.baby_steps, info.giant_steps, info.table_slots,
          info.primes_per_launch);
 
+  // Resume from a checkpoint of the same input and P1.
+  unsigned long long p = low;
+  if (ckpt) {
+    if (FILE *cf = fopen(ckpt, "r")) {
+      char line[4096];
+      unsigned long long next = 0, chigh = 0;
+      std::string cin;
+      while (fgets(line, sizeof(line), cf)) {
+        if (!strncmp(line, "next_p=", 7)) next = strtoull(line + 7, nullptr, 10);
+        else if (!strncmp(line, "high=", 5)) chigh = strtoull(line + 5, nullptr, 10);
+        else if (!strncmp(line, "abcd=", 5)) {
+          cin = line + 5;
+          while (!cin.empty() && (cin.back() == '\n' || cin.back() == '\r')) cin.pop_back();
+        }
+      }
+      fclose(cf);
+      if (chigh == high && cin == abcd && next > p) {
+        printf("Resuming from checkpoint %s at p=%llu\n", ckpt, next);
+        p = next;
+      }
+    }
+  }
+  auto save_ckpt = [&](unsigned long long next) {
+    if (!ckpt) return;
+    std::string tmp = std::string(ckpt) + ".tmp";
+    FILE *cf = fopen(tmp.c_str(), "w");
+    if (!cf) return;
+    fprintf(cf, "next_p=%llu\nhigh=%llu\nabcd=%s\n", next, high, abcd);
+    fclose(cf);
+    rename(tmp.c_str(), ckpt);
+  };
+
   // Progress granularity: ~20 launches' worth of primes per call.
   const auto t_start = std::chrono::high_resolution_clock::now();
-  unsigned long long p = low;
   unsigned long long total_factors = 0;
   std::vector<rs_factor> out(1 << 16);
   while (p <= high) {
@@ -149,6 +187,7 @@ int main(int argc, char **argv) {
       return 1;
     }
     total_factors += cnt;
+    save_ckpt(q + 1);
     const auto t1 = std::chrono::high_resolution_clock::now();
     const double dt = std::chrono::duration<double>(t1 - t0).count();
     const double so_far = std::chrono::duration<double>(t1 - t_start).count();
@@ -163,10 +202,42 @@ int main(int argc, char **argv) {
     if (q == high) break;
     p = q + 1;
   }
+  if (p > high) save_ckpt(high + 1);
   const double total = std::chrono::duration<double>(std::chrono::high_resolution_clock::now() - t_start).count();
   printf("\nTime taken: %gs\n", total);
   printf("Factors found: %llu\n", total_factors);
   printf("Progress = %llu at %.0f p/sec\n\n", high - low + 1, (double)(high - low + 1) / total);
   rs_job_destroy(job);
+
+  if (abcd_out) {
+    // every factor line of the factor file for this base and sign
+    std::vector<rs_factor> rm;
+    if (FILE *ff = fopen(factor_file, "r")) {
+      unsigned long long fp;
+      unsigned fk, fb, fn;
+      char sg;
+      char line[256];
+      while (fgets(line, sizeof(line), ff))
+        if (sscanf(line, "%llu | %u*%u^%u%c1", &fp, &fk, &fb, &fn, &sg) == 5 && fb == info.base &&
+            (sg == '-') == (info.sign < 0))
+          rm.push_back(rs_factor{fp, fk, fn});
+      fclose(ff);
+    }
+    size_t need = 0;
+    std::string out(text.size() + 4096 + 64 * (size_t)info.num_k, '\0');
+    rc = rs_abcd_remove(text.data(), text.size(), rm.data(), rm.size(), high, &out[0], out.size(), &need);
+    if (rc == RS_ERR_CAPACITY) {
+      out.resize(need);
+      rc = rs_abcd_remove(text.data(), text.size(), rm.data(), rm.size(), high, &out[0], out.size(), &need);
+    }
+    FILE *wf = rc ? nullptr : fopen(abcd_out, "w");
+    if (!wf || fwrite(out.data(), 1, need, wf) != need) {
+      fprintf(stderr, "error writing %s: %s\n", abcd_out, rc ? rs_last_error() : "I/O error");
+      if (wf) fclose(wf);
+      return 1;
+    }
+    fclose(wf);
+    printf("Wrote %s: %zu candidates removed\n", abcd_out, rm.size());
+  }
   return 0;
 }

@@ -1075,3 +1075,39 @@ extern "C" int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const ui
   if (e != cudaSuccess) return fail(RS_ERR_CUDA, "arith check: %s", cudaGetErrorString(e));
   return RS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Sieve-file update: the ABCD text with the removed candidates dropped.  The
+// reference only appends factor lines (kernel_v0.24.6.cu:1830-1835); srsieve
+// workflows continue from an updated ABCD file, which this writes.
+
+extern "C" int rs_abcd_remove(const char *text, size_t len, const rs_factor *removed, size_t count,
+                              uint64_t sieved_to, char *out, size_t cap, size_t *out_len) {
+  if (!text || !out_len || (!removed && count) || (!out && cap)) return fail(RS_ERR_INVALID, "NULL argument");
+  Seqs s;
+  int rc = parse_abcd(text, len, s);
+  if (rc) return rc;
+  normalise(s);
+  std::vector<std::pair<uint32_t, uint32_t>> rm(count);
+  for (size_t i = 0; i < count; i++) rm[i] = {removed[i].k, removed[i].n};
+  std::sort(rm.begin(), rm.end());
+  std::string o;
+  char buf[160];
+  for (size_t i = 0; i < s.k.size(); i++) {
+    std::vector<uint32_t> keep;
+    for (uint32_t n : s.n[i])
+      if (!std::binary_search(rm.begin(), rm.end(), std::make_pair(s.k[i], n))) keep.push_back(n);
+    if (keep.empty()) continue;
+    snprintf(buf, sizeof(buf), "ABCD %u*%u^$a%s [%u] // Sieved to %llu\n", s.k[i], s.base, s.sign < 0 ? "-1" : "+1",
+             keep[0], (unsigned long long)sieved_to);
+    o += buf;
+    for (size_t t = 1; t < keep.size(); t++) {
+      snprintf(buf, sizeof(buf), "%u\n", keep[t] - keep[t - 1]);
+      o += buf;
+    }
+  }
+  *out_len = o.size();
+  if (o.size() > cap) return fail(RS_ERR_CAPACITY, "output needs %zu bytes, buffer holds %zu", o.size(), cap);
+  memcpy(out, o.data(), o.size());
+  return RS_OK;
+}

@@ -29,6 +29,7 @@ EXPORTS = (
     "rs_options_default", "rs_job_create_abcd", "rs_job_create", "rs_job_info_get",
     "rs_plan_abcd", "rs_job_destroy", "rs_sieve_range", "rs_write_factors", "rs_gpu_primes",
     "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
+    "rs_abcd_remove",
 )
 
 
@@ -120,6 +121,7 @@ def lib():
                                     ctypes.POINTER(ctypes.c_double)]
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
         L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
+        L.rs_abcd_remove.argtypes = [ctypes.c_char_p, sz, vp, sz, u64, vp, sz, ctypes.POINTER(sz)]
         L.rs_last_error.restype = ctypes.c_char_p
         L.rs_version.restype = ctypes.c_char_p
         _lib = L
@@ -212,6 +214,23 @@ class Job:
             self.close()
         except Exception:
             pass
+
+
+def abcd_remove(text: str | bytes, removed, sieved_to: int) -> str:
+    """ABCD text with the (k, n) of `removed` (array with fields k, n) dropped (host only)."""
+    if isinstance(text, str):
+        text = text.encode()
+    f = np.ascontiguousarray(removed, dtype=FACTOR_DTYPE) if len(removed) else np.zeros(0, FACTOR_DTYPE)
+    cap = len(text) + 4096 + 64 * text.count(b"ABCD")
+    while True:
+        out = ctypes.create_string_buffer(cap)
+        n = ctypes.c_size_t(0)
+        rc = lib().rs_abcd_remove(text, len(text), f.ctypes.data, len(f), sieved_to, out, cap, ctypes.byref(n))
+        if rc == RS_ERR_CAPACITY:
+            cap = n.value
+            continue
+        _check(rc)
+        return out.raw[: n.value].decode()
 
 
 def gpu_primes(lo: int, hi: int, device: int = 0) -> np.ndarray:

@@ -130,6 +130,14 @@ int rs_sieve_range(rs_job *job, uint64_t p0, uint64_t p1, rs_factor *out, size_t
  * (kernel_v0.24.6.cu:1830-1835; "+1" for a Sierpinski job). */
 int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, size_t count);
 
+/* Sieve-file update (srsieve workflow; the reference only appends factor lines,
+ * kernel_v0.24.6.cu:1830-1835): the ABCD text with every (k, n) in `removed`
+ * dropped, k with no candidate left omitted, and "// Sieved to <sieved_to>" on
+ * each header.  Host only.  RS_ERR_CAPACITY with *out_len = bytes needed when
+ * cap is too small. */
+int rs_abcd_remove(const char *text, size_t len, const rs_factor *removed, size_t count, uint64_t sieved_to,
+                   char *out, size_t cap, size_t *out_len);
+
 /* The device prime sieve alone: odd primes in [lo, hi], ascending (replaces the
  * host generateGPUPrimes, kernel_v0.24.6.cu:1838-1987).  Returns
  * RS_ERR_CAPACITY with *count = needed when cap is too small. */

@@ -99,3 +99,27 @@ def test_cli_help(rs):
 def test_cli_rejects_odd_q(rs, tmp_path):
     out = subprocess.run([rs.CLI, "-Q", "3"], capture_output=True, text=True, cwd=tmp_path)
     assert out.returncode == 1 and "Q must be an even integer" in out.stdout
+
+
+def test_abcd_remove_round_trip(rs, oracle_mod, sr745_text):
+    """Sieve-file update: removed (k, n) disappear, everything else survives."""
+    import numpy as np
+
+    job = oracle_mod.Job.from_abcd(sr745_text)
+    ks = job.ks
+    removed = [(ks[0], int(job.nlist(0)[0])), (ks[0], int(job.nlist(0)[5])), (ks[3], int(job.nlist(3)[-1]))]
+    # a k whose every candidate is removed disappears
+    tiny = "ABCD 3*2^$a-1 [10]\n2\nABCD 5*2^$a-1 [11]\n"
+    out_tiny = rs.abcd_remove(tiny, np.array([(0, 5, 11)], dtype=rs.FACTOR_DTYPE), 10**9)
+    assert "5*2" not in out_tiny and out_tiny.startswith("ABCD 3*2^$a-1 [10] // Sieved to 1000000000\n2\n")
+    f = np.array([(0, k, n) for k, n in removed], dtype=rs.FACTOR_DTYPE)
+    out = rs.abcd_remove(sr745_text, f, 6 * 10**12)
+    assert out.count("// Sieved to 6000000000000") == 22
+    job2 = oracle_mod.Job.from_abcd(out)
+    assert job2.ks == ks
+    for i in range(len(ks)):
+        want = set(job.nlist(i).tolist()) - {n for k, n in removed if k == ks[i]}
+        assert set(job2.nlist(i).tolist()) == want
+    # nothing removed: identical candidate sets
+    job3 = oracle_mod.Job.from_abcd(rs.abcd_remove(sr745_text, [], 1))
+    assert all(np.array_equal(job3.nlist(i), job.nlist(i)) for i in range(len(ks)))

@@ -174,3 +174,29 @@ def test_every_factor_verifies_at_scale(rs, oracle_mod):
         assert (k, n) in cand
     assert st["primes"] > 3 * 10**8
     job.close()
+
+
+def test_wide_config_window(rs, oracle_mod):
+    """The wide workload (b=2, 1000 k in [3, 1e7], n in [1e6, 3e6] at 2%) on a
+    2e6-wide window at 2^50, complete and datless."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.wide_job(1)
+    p0 = S.WIDE_RANGE[0]
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**6, datless=datless)
+        assert g == o
+    assert st["primes"] > 50000
+
+
+@pytest.mark.parametrize("i", [0, 1, 2, 3])
+def test_batch_shaped_jobs(rs, oracle_mod, i):
+    """Jobs drawn from the mixed-batch distribution (random base, k count,
+    n range, density, p window up to 2^60), on a narrow window each."""
+    import rsieve.synth as S
+
+    (b, s, ks, nl), (p0, p1) = S.batch_job(7, i)
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**6, 10**6 + 3 * 10**5, datless=True)
+    assert g == o and len(o) > 0
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 3 * 10**5, datless=True)
+    assert g == o and st["primes"] > 1000
