@@ -42,10 +42,9 @@ __device__ __forceinline__ uint64_t montmul(uint64_t a, uint64_t b, const Mont &
 // Montgomery product above.
 __device__ __forceinline__ uint64_t shoup_mul(uint64_t x, uint64_t w, uint64_t wq, uint64_t p) {
   const uint64_t q = __umul64hi(x, wq);
-  uint64_t r = x * w - q * p;
-  r -= p;
-  r += p & (uint64_t)((int64_t)r >> 63);
-  return r;
+  const uint64_t r = x * w + q * (0 - p);  // x*w - q*p, a multiply-add chain
+  const uint64_t t = r - p;
+  return (int64_t)t < 0 ? r : t;
 }
 
 // floor(w * 2^64 / p) from the Montgomery form wm = w * 2^64 mod p: since

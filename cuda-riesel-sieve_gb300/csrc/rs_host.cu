@@ -272,7 +272,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
   pl.e0 = (int64_t)pl.x_lo - 1;
   pl.jbits = 1;
   while (((uint64_t)1 << pl.jbits) < (uint64_t)pl.m + 1) pl.jbits++;
-  // fast-path buckets: kBucket 16-bit tags each, at most half full on average
+  // fast-path buckets: 7 16-bit tags each, at most about 2/7 full on average
   pl.bucket_log2 = std::max<uint32_t>(4, ilog2_ceil((2 * (uint64_t)pl.m + kBucket - 1) / kBucket));
   pl.words_per_row = (pl.X + 31) / 32;
   // rows: k in input order, r ascending
@@ -454,7 +454,7 @@ static int upload_job(rs_job *j) {
     d.stage_full = 0;
     d.stage_elems = kElV;
   }
-  d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
+  d.warp_smem = (uint32_t)align_up((16u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.k_val = (const uint32_t *)(b + o_kv);

@@ -24,12 +24,14 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // by the BSGS kernel: rec_elems (even) 64-bit elements per prime, contiguous,
 // element e of prime i at recs[i * rec_elems + e], so the BSGS kernel stages a
 // record with 16-byte cp.async copies of whole sectors.  Element map:
-//   0 p, 1 pinv, 2 B^32 (baby stride), 3 G^32 (giant stride), 4 nact | flags<<32,
-//   5..7 unused, 8..39 B^lane, 40..71 G^(lane % tlanes + 1),
-//   72.. V[max_act] (giant-step start per active row), then row ids (u16, 4 per element).
-// All residues are in Montgomery form.
+//   0 p, 1 pinv, 2 B^32 (baby stride), 3 G^32 (giant stride), 4 nact,
+//   6,7 B^64 in normal form and its Shoup constant, 8,9 B^32 likewise,
+//   10,11 G^32 likewise, 16..47 B^lane, 48..79 G^(lane % tlanes + 1),
+//   80.. V[max_act] (giant-step start per active row), then row ids (u16, 4 per element).
+// Residues are in Montgomery form unless marked normal.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBs = 2, kElGs = 3, kElNact = 4;
-constexpr uint32_t kElB = 8, kElG = 40, kElV = 72;
+constexpr uint32_t kElB2w = 6, kElB2q = 7, kElBw = 8, kElBq = 9, kElGw = 10, kElGq = 11;
+constexpr uint32_t kElB = 16, kElG = 48, kElV = 80;
 
 // Job constants, passed by value to every kernel (lives in the constant bank).
 struct JobDev {

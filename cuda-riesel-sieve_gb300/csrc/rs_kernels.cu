@@ -27,13 +27,11 @@ namespace rs {
 
 // ---------------------------------------------------------------------------
 // Segmented sieve of Eratosthenes over the odd numbers of [lo, hi], lo odd.
-// Bit x of the window stands for lo + 2x.  Sieving primes q >= kSieveLarge hit a
+// Bit x of the window stands for lo + 2x.  Sieving primes q >= 2*kSieveOdds hit a
 // 2^15-odd segment at most once or twice, so they are applied once per window
 // by sieve_large_kernel (one thread per prime, atomicOr into an L2-resident
 // bitmap of the whole window); sieve_small_kernel then starts each segment from
 // that bitmap, crosses off the small primes in shared memory and compacts.
-
-constexpr uint32_t kSieveLarge = 2 * kSieveOdds;  // q at or above this: bucket pass
 
 __global__ void __launch_bounds__(256) sieve_large_kernel(uint64_t lo, uint64_t hi, const uint32_t *__restrict__ sp,
                                                           const uint64_t *__restrict__ sp_rcp, uint32_t first,
@@ -317,6 +315,13 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBs, Bs, Gs);
   rec_st2(rec, kElNact, nact, 0);
+  {
+    // the strides in normal form with their Shoup constants, once per prime
+    const uint64_t B2 = montmul(Bs, Bs, M);  // B^64
+    rec_st2(rec, kElB2w, montmul(B2, 1, M), shoup_const(B2, M.pinv));
+    rec_st2(rec, kElBw, montmul(Bs, 1, M), shoup_const(Bs, M.pinv));
+    rec_st2(rec, kElGw, montmul(Gs, 1, M), shoup_const(Gs, M.pinv));
+  }
 }
 
 // Quadratic-character tables: word w of the table of odd k' holds bit t =
@@ -401,47 +406,67 @@ struct __align__(16) Match {
   uint32_t s;     // giant index
 };
 
-// 16-bit tag of a residue: bits [tl, tl+16) of its low word, above the
-// bucket index (tl <= 16), never 0 (0 marks an empty slot).
-__device__ __forceinline__ uint32_t tag16(uint64_t v, uint32_t tl) {
-  return max(((uint32_t)v >> tl) & 0xffffu, 1u);
-}
+// 16-bit tag of a residue: the high half of its low word (the bucket index
+// uses the low log2(NB) <= 16 bits), never 0 (0 marks an empty slot).
+__device__ __forceinline__ uint32_t tag16(uint32_t lo) { return max(lo >> 16, 1u); }
 
-// True iff one of the 8 tags of bucket q equals the tag pair T = t*0x10001.
+// Bucket layout: 16 bytes, slots 0..6 hold 16-bit tags (0 = empty), slot 7 (the
+// high half of the last word) counts insert attempts.  True iff one of the 7
+// tags equals the tag pair T = t*0x10001.  The count half is forced to 0xffff,
+// so it can only match the tag 0xffff: a false match, which the exact
+// comparison after the giant steps discards.
 __device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
-  const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
-  return (m & 0xffffu) == 0 || (m >> 16) == 0;
+  const uint32_t m =
+      __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, (q.w | 0xffff0000u) ^ T));
+  return (m & 0xffffu) == 0 || m < 0x10000u;
 }
 
-// Hash-table view of one warp's shared memory.
+constexpr uint32_t kSlots = 7;                  // tag slots per bucket
+constexpr uint32_t kFull = kSlots << 16;        // count half >= 7: bucket full
+
+// Hash-table view of one warp's shared memory.  An insert takes the next slot
+// of its bucket with an atomic add on the bucket's count half; slots 0..5 are
+// written with a plain 16-bit store, slot 6 (which shares the count's word)
+// with an atomic OR.  Slots fill in order, so a bucket is full iff its count
+// reached 7, and an entry overflows into bucket b+1 only when bucket b is full:
+// a probe scans from the home bucket to the first bucket that is not full.
 struct WarpTable {
   uint4 *tab4;
+  uint32_t *tab32;
   uint16_t *tab16;
-  uint32_t *cnt;
-  uint32_t bmask, tl;
+  uint32_t bmask;
 
   __device__ __forceinline__ void insert(uint64_t v) const {
-    uint32_t b = (uint32_t)v & bmask;
-    uint32_t c = atomicAdd(&cnt[b], 1u);
+    const uint32_t lo = (uint32_t)v;
+    uint32_t b = lo & bmask;
+    uint32_t c = atomicAdd(&tab32[b * 4 + 3], 0x10000u) >> 16;
+    if (c >= kSlots) {  // rare: the home bucket is full
 #pragma unroll 1
-    for (uint32_t g = 0; c >= (uint32_t)kBucket && g <= bmask; g++) {
-      b = (b + 1) & bmask;
-      c = atomicAdd(&cnt[b], 1u);
+      for (uint32_t g = 0; c >= kSlots && g < bmask; g++) {
+        b = (b + 1) & bmask;
+        c = atomicAdd(&tab32[b * 4 + 3], 0x10000u) >> 16;
+      }
     }
-    if (c < (uint32_t)kBucket) tab16[b * kBucket + c] = (uint16_t)tag16(v, tl);
+    const uint32_t t = tag16(lo);
+    if (c < kSlots - 1) tab16[b * 8 + c] = (uint16_t)t;
+    else if (c == kSlots - 1) atomicOr(&tab32[b * 4 + 3], t);
   }
 
   // True iff some entry with the tag of y lies in y's probe sequence.
   __device__ __forceinline__ bool probe(uint64_t y) const {
-    uint32_t b = (uint32_t)y & bmask;
-    const uint32_t T = tag16(y, tl) * 0x10001u;
-    bool hit = false;
+    const uint32_t lo = (uint32_t)y;
+    uint32_t b = lo & bmask;
+    const uint32_t T = tag16(lo) * 0x10001u;
+    uint4 q = tab4[b];
+    bool hit = bucket_has(q, T);
+    if (q.w >= kFull) {  // rare: the home bucket is full, continue scanning
 #pragma unroll 1
-    for (uint32_t g = 0; g <= bmask; g++) {
-      const uint4 q = tab4[b];
-      hit |= bucket_has(q, T);
-      if (q.w < 0x10000u) break;  // slot 7 empty: not full, the probe ends here
-      b = (b + 1) & bmask;
+      for (uint32_t g = 0; g < bmask; g++) {
+        b = (b + 1) & bmask;
+        q = tab4[b];
+        hit |= bucket_has(q, T);
+        if (q.w < kFull) break;
+      }
     }
     return hit;
   }
@@ -463,11 +488,7 @@ struct MatchList {
 };
 
 // Per-warp shared memory of the fast kernel:
-//   [NB buckets x 16 B][NB counters x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
-// Buckets fill slot 0..7 in order (a per-bucket atomic counter hands out slots),
-// so a bucket is full iff its slot 7 is nonzero, and an entry overflows into
-// bucket b+1 only when bucket b is full: a probe scans from the home bucket to
-// the first bucket that is not full.
+//   [NB buckets x 16 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
 //
 // Each lane runs two independent product chains in both phases (baby steps
 // j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
@@ -483,11 +504,10 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * J.warp_smem;
   WarpTable W;
   W.tab4 = reinterpret_cast<uint4 *>(base);
+  W.tab32 = reinterpret_cast<uint32_t *>(base);
   W.tab16 = reinterpret_cast<uint16_t *>(base);
-  W.cnt = reinterpret_cast<uint32_t *>(base + NB * 16);
   W.bmask = NB - 1;
-  W.tl = J.table_log2;
-  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
+  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 16);
   MatchList ML;
   ML.list = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
@@ -518,55 +538,67 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       const uint64_t p = cur[kElP], pinv = cur[kElPinv];
       // Multipliers in normal form with their Shoup constants; the values
       // they multiply stay in Montgomery form, so products stay comparable.
-      const uint64_t Bm = cur[kElBs], Gm = cur[kElGs];
-      const uint64_t B2m = montmul(Bm, Bm, p, pinv);  // B^64
-      const uint64_t Bw = montmul(Bm, 1, p, pinv), Bq = shoup_const(Bm, pinv);
-      const uint64_t B2w = montmul(B2m, 1, p, pinv), B2q = shoup_const(B2m, pinv);
-      const uint64_t Gw = montmul(Gm, 1, p, pinv), Gq = shoup_const(Gm, pinv);
+      const uint64_t Bw = cur[kElBw], Bq = cur[kElBq], B2w = cur[kElB2w], B2q = cur[kElB2q];
+      const uint64_t Gw = cur[kElGw], Gq = cur[kElGq];
       const uint64_t Glm = cur[kElG + lane];
       const uint64_t Glw = montmul(Glm, 1, p, pinv), Glq = shoup_const(Glm, pinv);
       const uint64_t Bl = cur[kElB + lane];
       const uint64_t Bl32 = shoup_mul(Bl, Bw, Bq, p);  // B^(lane+32)
-      // clear the table and the bucket counters
+      // clear the table (tags and counts)
       const uint4 z4 = make_uint4(0, 0, 0, 0);
-      for (uint32_t q = lane; q < NB + NB / 4; q += 32) W.tab4[q] = z4;
+      for (uint32_t q = lane; q < NB; q += 32) W.tab4[q] = z4;
       if (lane == 0) *ML.count = 0;
       __syncwarp();
 
       // Baby steps: chain A owns j = lane + 64t, chain B j = lane + 32 + 64t.
       {
         uint64_t va = Bl, vb = Bl32;
+        const uint32_t nfull = J.m / 64;  // iterations where every lane inserts twice
 #pragma unroll 1
-        for (uint32_t t = 0; t < nbaby2; t++) {
-          const uint32_t ja = lane + 64 * t;
-          if (ja < J.m) W.insert(va);
-          if (ja + 32 < J.m) W.insert(vb);
+        for (uint32_t t = 0; t < nfull; t++) {
+          W.insert(va);
+          W.insert(vb);
           va = shoup_mul(va, B2w, B2q, p);
           vb = shoup_mul(vb, B2w, B2q, p);
         }
+        const uint32_t ja = lane + 64 * nfull;
+        if (ja < J.m) W.insert(va);
+        if (ja + 32 < J.m) W.insert(vb);
       }
       __syncwarp();
 
       // Giant steps: lane (lane_row, lane_t) takes row slots g*RPI + lane_row for
       // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
       const uint32_t ngi = (nact + RPI - 1) / RPI;
+      const uint64_t *Vs = J.stage_full ? cur + kElV : cb.recs + (size_t)i * J.rec_elems + kElV;
+      if (spl == 1) {
 #pragma unroll 1
-      for (uint32_t gi = 0; gi < ngi; gi += 2) {
-        const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
-        const bool aa = sa < nact, ab = sb < nact;
-        const uint64_t Va = J.stage_full ? cur[kElV + (aa ? sa : 0)] : rec_el(J, cb, kElV + (aa ? sa : 0), i);
-        const uint64_t Vb = J.stage_full ? cur[kElV + (ab ? sb : 0)] : rec_el(J, cb, kElV + (ab ? sb : 0), i);
-        uint64_t ya = shoup_mul(Va, Glw, Glq, p);
-        uint64_t yb = shoup_mul(Vb, Glw, Glq, p);
-        uint32_t s = lane_t + 1;
+        for (uint32_t gi = 0; gi < ngi; gi += 2) {
+          const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
+          const uint64_t ya = shoup_mul(Vs[min(sa, nact - 1)], Glw, Glq, p);
+          const uint64_t yb = shoup_mul(Vs[min(sb, nact - 1)], Glw, Glq, p);
+          const bool ha = W.probe(ya) && sa < nact;
+          const bool hb = W.probe(yb) && sb < nact;
+          if (ha) ML.push(ya, sa, lane_t + 1);
+          if (hb) ML.push(yb, sb, lane_t + 1);
+        }
+      } else {
 #pragma unroll 1
-        for (uint32_t u = 0;; u++) {
-          if (aa && W.probe(ya)) ML.push(ya, sa, s);
-          if (ab && W.probe(yb)) ML.push(yb, sb, s);
-          if (u + 1 >= spl) break;
-          ya = shoup_mul(ya, Gw, Gq, p);
-          yb = shoup_mul(yb, Gw, Gq, p);
-          s += 32;
+        for (uint32_t gi = 0; gi < ngi; gi += 2) {
+          const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
+          const bool aa = sa < nact, ab = sb < nact;
+          uint64_t ya = shoup_mul(Vs[min(sa, nact - 1)], Glw, Glq, p);
+          uint64_t yb = shoup_mul(Vs[min(sb, nact - 1)], Glw, Glq, p);
+          uint32_t s = lane_t + 1;
+#pragma unroll 1
+          for (uint32_t u = 0;; u++) {
+            if (W.probe(ya) && aa) ML.push(ya, sa, s);
+            if (W.probe(yb) && ab) ML.push(yb, sb, s);
+            if (u + 1 >= spl) break;
+            ya = shoup_mul(ya, Gw, Gq, p);
+            yb = shoup_mul(yb, Gw, Gq, p);
+            s += 32;
+          }
         }
       }
       __syncwarp();
