@@ -35,6 +35,14 @@ __device__ __forceinline__ uint64_t montmul(uint64_t a, uint64_t b, const Mont &
   return montmul(a, b, m.p, m.pinv);
 }
 
+// x*2^-64 mod p for x < p (leaving Montgomery form): the Montgomery product by 1
+// with its zero high word dropped.  With m = x*pinv mod 2^64, m*p == -x (mod 2^64),
+// so x + m*p = umulhi(m, p)*2^64 + 2^64 when x != 0: the result is
+// umulhi(m, p) + 1, already below p (it equals p only for x == 0 mod p).
+__device__ __forceinline__ uint64_t from_mont(uint64_t x, uint64_t p, uint64_t pinv) {
+  return x ? __umul64hi(x * pinv, p) + 1 : 0;
+}
+
 // Shoup's product x*w mod p for a fixed multiplier w < p with
 // wq = floor(w * 2^64 / p); any x < 2^64; p < 2^63.  The quotient estimate
 // umulhi(x, wq) is at most one short, so r = x*w - q*p lies in [0, 2p) and one

@@ -446,15 +446,16 @@ static int upload_job(rs_job *j) {
   d.datless = j->opt.datless ? 1u : 0u;
   d.max_act = std::max<uint32_t>(1, pl.nrows);
   d.el_row = kElV + ((d.max_act + 1) & ~1u);  // even: row ids are written 16 bytes at a time
-  d.rec_elems = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
-  if (d.rec_elems * 8 <= 4096) {
+  d.el_tab = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
+  d.rec_elems = d.el_tab + 64;
+  if (d.el_row * 8 <= 2048) {
     d.stage_full = 1;
-    d.stage_elems = d.rec_elems;
+    d.stage_elems = d.el_row;
   } else {
     d.stage_full = 0;
     d.stage_elems = kElV;
   }
-  d.warp_smem = (uint32_t)align_up((16u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
+  d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.k_val = (const uint32_t *)(b + o_kv);

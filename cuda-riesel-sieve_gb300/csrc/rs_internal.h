@@ -11,7 +11,7 @@ namespace rs {
 // BSGS fast path: per-prime hash of 16-bit tags, kBucket tags per 16-byte bucket.
 constexpr uint32_t kEmptyTag = 0xffffu;
 constexpr int kBucket = 8;
-constexpr int kMatchCap = 32;       // deferred tag matches per prime before the exact path
+constexpr int kMatchCap = 16;       // deferred tag matches per prime before the exact path
 // BSGS exact path (rare primes): 32-bit entries (tag << jbits) | j, linear probing.
 // j <= m-1 <= 2^jbits - 2, so a real entry is never all ones.
 constexpr uint32_t kEmpty = 0xffffffffu;
@@ -20,18 +20,20 @@ constexpr int kSieveOdds = 1 << 15; // odd numbers per sieve segment (4 KB of bi
 constexpr int kSieveThreads = 256;
 constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for this k
 
-// Per-prime records, written by the setup kernel and staged into shared memory
-// by the BSGS kernel: rec_elems (even) 64-bit elements per prime, contiguous,
-// element e of prime i at recs[i * rec_elems + e], so the BSGS kernel stages a
-// record with 16-byte cp.async copies of whole sectors.  Element map:
+// Per-prime records, written by the setup kernel and read by the BSGS kernel:
+// rec_elems (even) 64-bit elements per prime, contiguous, element e of prime i
+// at recs[i * rec_elems + e].  The BSGS kernel stages the header and V (the
+// first el_row elements) into shared memory with 16-byte cp.async copies and
+// loads each lane's own table entries straight into registers.  Element map:
 //   0 p, 1 pinv, 2 B^32 (baby stride), 3 G^32 (giant stride), 4 nact,
 //   6,7 B^64 in normal form and its Shoup constant, 8,9 B^32 likewise,
-//   10,11 G^32 likewise, 16..47 B^lane, 48..79 G^(lane % tlanes + 1),
-//   80.. V[max_act] (giant-step start per active row), then row ids (u16, 4 per element).
+//   10,11 G^32 likewise, 12.. V[max_act] (giant-step start per active row),
+//   el_row.. row ids (u16, 4 per element), el_tab.. B^lane (32 elements),
+//   el_tab+32.. G^(lane % tlanes + 1) (32 elements).
 // Residues are in Montgomery form unless marked normal.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBs = 2, kElGs = 3, kElNact = 4;
 constexpr uint32_t kElB2w = 6, kElB2q = 7, kElBw = 8, kElBq = 9, kElGw = 10, kElGq = 11;
-constexpr uint32_t kElB = 16, kElG = 48, kElV = 80;
+constexpr uint32_t kElV = 12;
 
 // Job constants, passed by value to every kernel (lives in the constant bank).
 struct JobDev {
@@ -54,6 +56,7 @@ struct JobDev {
   uint32_t max_act;      // capacity of the per-prime active-row arrays (= nrows)
   uint32_t rec_elems;    // 64-bit elements per prime record
   uint32_t el_row;       // first element of the row-id array
+  uint32_t el_tab;       // first element of the per-lane tables (B^lane, then G^(lane % tlanes + 1))
   uint32_t stage_elems;  // elements of a record staged in shared memory (all, or the first kElV)
   uint32_t stage_full;   // 1 if V and row ids are read from the staged copy
   uint32_t warp_smem;    // shared-memory bytes per warp in the fast BSGS kernel

@@ -212,26 +212,26 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   // stepped with Shoup products by the fixed B and G.
   uint64_t Bs, Gs = 0;
   {
-    const uint64_t Bw = montmul(B, 1, M), Bq = shoup_const(B, M.pinv);
+    const uint64_t Bw = from_mont(B, p, M.pinv), Bq = shoup_const(B, M.pinv);
     uint64_t v = one;
 #pragma unroll 4
     for (uint32_t l = 0; l < 32; l += 2) {
       const uint64_t v1 = shoup_mul(v, Bw, Bq, p);
-      rec_st2(rec, kElB + l, v, v1);
+      rec_st2(rec, J.el_tab + l, v, v1);
       v = shoup_mul(v1, Bw, Bq, p);
     }
     Bs = v;  // B^32
-    const uint64_t Gw = montmul(G, 1, M), Gq = shoup_const(G, M.pinv);
+    const uint64_t Gw = from_mont(G, p, M.pinv), Gq = shoup_const(G, M.pinv);
     if (J.tlanes == 1) {
 #pragma unroll 1
-      for (uint32_t l = 0; l < 32; l += 2) rec_st2(rec, kElG + l, G, G);
+      for (uint32_t l = 0; l < 32; l += 2) rec_st2(rec, J.el_tab + 32 + l, G, G);
     } else {
       uint64_t g = G;
 #pragma unroll 1
       for (uint32_t l = 0; l < J.tlanes; l += 2) {
         const uint64_t g1 = shoup_mul(g, Gw, Gq, p);
 #pragma unroll 1
-        for (uint32_t c = l; c < 32; c += J.tlanes) rec_st2(rec, kElG + c, g, g1);
+        for (uint32_t c = l; c < 32; c += J.tlanes) rec_st2(rec, J.el_tab + 32 + c, g, g1);
         if (l == 30) Gs = g1;  // G^32
         g = shoup_mul(g1, Gw, Gq, p);
       }
@@ -318,9 +318,9 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   {
     // the strides in normal form with their Shoup constants, once per prime
     const uint64_t B2 = montmul(Bs, Bs, M);  // B^64
-    rec_st2(rec, kElB2w, montmul(B2, 1, M), shoup_const(B2, M.pinv));
-    rec_st2(rec, kElBw, montmul(Bs, 1, M), shoup_const(Bs, M.pinv));
-    rec_st2(rec, kElGw, montmul(Gs, 1, M), shoup_const(Gs, M.pinv));
+    rec_st2(rec, kElB2w, from_mont(B2, p, M.pinv), shoup_const(B2, M.pinv));
+    rec_st2(rec, kElBw, from_mont(Bs, p, M.pinv), shoup_const(Bs, M.pinv));
+    rec_st2(rec, kElGw, from_mont(Gs, p, M.pinv), shoup_const(Gs, M.pinv));
   }
 }
 
@@ -400,6 +400,8 @@ __device__ __forceinline__ void stage_commit_empty() { asm volatile("cp.async.co
 __device__ __forceinline__ void stage_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+constexpr int kOvfCap = 2 * kMatchCap;  // 8-byte values in the match list's space
+
 struct __align__(16) Match {
   uint64_t y;     // giant-step value whose tag matched
   uint32_t slot;  // active-row slot
@@ -410,46 +412,59 @@ struct __align__(16) Match {
 // uses the low log2(NB) <= 16 bits), never 0 (0 marks an empty slot).
 __device__ __forceinline__ uint32_t tag16(uint32_t lo) { return max(lo >> 16, 1u); }
 
-// Bucket layout: 16 bytes, slots 0..6 hold 16-bit tags (0 = empty), slot 7 (the
-// high half of the last word) counts insert attempts.  True iff one of the 7
-// tags equals the tag pair T = t*0x10001.  The count half is forced to 0xffff,
-// so it can only match the tag 0xffff: a false match, which the exact
-// comparison after the giant steps discards.
+// Bucket layout: 16 bytes = eight 16-bit tags (0 = empty).  True iff one of
+// the 8 tags equals the tag pair T = t*0x10001.
 __device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
-  const uint32_t m =
-      __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, (q.w | 0xffff0000u) ^ T));
+  const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
   return (m & 0xffffu) == 0 || m < 0x10000u;
 }
 
-constexpr uint32_t kSlots = 7;                  // tag slots per bucket
-constexpr uint32_t kFull = kSlots << 16;        // count half >= 7: bucket full
+constexpr uint32_t kSlots = 8;  // tag slots per bucket
 
-// Hash-table view of one warp's shared memory.  An insert takes the next slot
-// of its bucket with an atomic add on the bucket's count half; slots 0..5 are
-// written with a plain 16-bit store, slot 6 (which shares the count's word)
-// with an atomic OR.  Slots fill in order, so a bucket is full iff its count
-// reached 7, and an entry overflows into bucket b+1 only when bucket b is full:
-// a probe scans from the home bucket to the first bucket that is not full.
+// Hash-table view of one warp's shared memory: NB buckets of tags and NB 32-bit
+// insert counts, kept apart from the buckets so that the counts of a warp's 32
+// random buckets spread over all 32 banks.  An insert takes slot c of its
+// bucket from an atomic add on the bucket's count and writes its tag there with
+// a plain 16-bit store.  Slots fill in order, so a bucket is full iff its slot 7
+// holds a tag, and an entry overflows into bucket b+1 only when bucket b is
+// full: a probe scans from the home bucket to the first bucket that is not full.
 struct WarpTable {
   uint4 *tab4;
-  uint32_t *tab32;
   uint16_t *tab16;
+  uint32_t *cnt32;
   uint32_t bmask;
 
-  __device__ __forceinline__ void insert(uint64_t v) const {
-    const uint32_t lo = (uint32_t)v;
-    uint32_t b = lo & bmask;
-    uint32_t c = atomicAdd(&tab32[b * 4 + 3], 0x10000u) >> 16;
-    if (c >= kSlots) {  // rare: the home bucket is full
+  __device__ __forceinline__ uint32_t take(uint32_t b) const {
+    return atomicAdd(&cnt32[b], 1u);
+  }
+
+  // Insert continuing after bucket b, whose slots are all taken.
+  __device__ __forceinline__ void insert_after(uint32_t lo, uint32_t b) const {
+    uint32_t c = kSlots;
 #pragma unroll 1
-      for (uint32_t g = 0; c >= kSlots && g < bmask; g++) {
-        b = (b + 1) & bmask;
-        c = atomicAdd(&tab32[b * 4 + 3], 0x10000u) >> 16;
-      }
+    for (uint32_t g = 0; c >= kSlots && g < bmask; g++) {
+      b = (b + 1) & bmask;
+      c = take(b);
     }
-    const uint32_t t = tag16(lo);
-    if (c < kSlots - 1) tab16[b * 8 + c] = (uint16_t)t;
-    else if (c == kSlots - 1) atomicOr(&tab32[b * 4 + 3], t);
+    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag16(lo);
+  }
+
+  // Insert into the home bucket; false if it was full (the caller finishes the
+  // insert later with insert_after, keeping the rare overflow off the hot loop).
+  __device__ __forceinline__ bool insert_home(uint64_t v) const {
+    const uint32_t lo = (uint32_t)v;
+    const uint32_t b = lo & bmask;
+    const uint32_t c = take(b);
+    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag16(lo);
+    return c < kSlots;
+  }
+
+  // Home-bucket test: true if the tag of y is in y's home bucket or that bucket
+  // is full (then only probe() can tell).
+  __device__ __forceinline__ bool probe_home(uint64_t y) const {
+    const uint32_t lo = (uint32_t)y;
+    const uint4 q = tab4[lo & bmask];
+    return bucket_has(q, tag16(lo) * 0x10001u) || q.w >= 0x10000u;
   }
 
   // True iff some entry with the tag of y lies in y's probe sequence.
@@ -459,13 +474,13 @@ struct WarpTable {
     const uint32_t T = tag16(lo) * 0x10001u;
     uint4 q = tab4[b];
     bool hit = bucket_has(q, T);
-    if (q.w >= kFull) {  // rare: the home bucket is full, continue scanning
+    if (q.w >= 0x10000u) {  // the home bucket is full, continue scanning
 #pragma unroll 1
       for (uint32_t g = 0; g < bmask; g++) {
         b = (b + 1) & bmask;
         q = tab4[b];
         hit |= bucket_has(q, T);
-        if (q.w < kFull) break;
+        if (q.w < 0x10000u) break;
       }
     }
     return hit;
@@ -475,6 +490,11 @@ struct WarpTable {
 struct MatchList {
   Match *list;
   uint32_t *count;
+  // Baby-phase use of the same space: up to kOvfCap values to insert late.
+  __device__ __forceinline__ void append(uint64_t *ovf, uint64_t v) const {
+    const uint32_t idx = atomicAdd(count, 1u);
+    if (idx < (uint32_t)kOvfCap) ovf[idx] = v;
+  }
   __device__ __forceinline__ void push(uint64_t y, uint32_t slot, uint32_t s) const {
     const uint32_t idx = atomicAdd(count, 1u);
     if (idx < (uint32_t)kMatchCap) {
@@ -488,7 +508,9 @@ struct MatchList {
 };
 
 // Per-warp shared memory of the fast kernel:
-//   [NB buckets x 16 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
+//   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
+// The stages hold a record's header and V (double-buffered with cp.async); each
+// lane's B^lane and G^(lane+1) entries are loaded into registers one prime ahead.
 //
 // Each lane runs two independent product chains in both phases (baby steps
 // j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
@@ -504,10 +526,10 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * J.warp_smem;
   WarpTable W;
   W.tab4 = reinterpret_cast<uint4 *>(base);
-  W.tab32 = reinterpret_cast<uint32_t *>(base);
   W.tab16 = reinterpret_cast<uint16_t *>(base);
+  W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
   W.bmask = NB - 1;
-  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 16);
+  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
   MatchList ML;
   ML.list = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
@@ -519,9 +541,16 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
   const uint32_t nbaby2 = (J.m + 63) / 64;  // iterations of the two-chain baby loop
   const uint32_t spl = J.steps_per_lane;
+  const uint64_t *ltab = cb.recs + J.el_tab + lane;  // this lane's B^lane; G^(lane+1) 32 further
 
-  if (first < n) stage_copy(stage0, J, cb, first, J.stage_elems, lane);
-  else stage_commit_empty();
+  uint64_t nBl = 0, nGl = 0;
+  if (first < n) {
+    stage_copy(stage0, J, cb, first, J.stage_elems, lane);
+    nBl = __ldg(ltab + (size_t)first * J.rec_elems);
+    nGl = __ldg(ltab + (size_t)first * J.rec_elems + 32);
+  } else {
+    stage_commit_empty();
+  }
 
 #pragma unroll 1
   for (uint32_t it = 0;; it++) {
@@ -529,8 +558,14 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     if (i >= n) break;
     const uint64_t *cur = stage0 + (it & 1) * J.stage_elems;
     uint64_t *nxt = stage0 + ((it + 1) & 1) * J.stage_elems;
-    if (i + nwarps < n) stage_copy(nxt, J, cb, i + nwarps, J.stage_elems, lane);
-    else stage_commit_empty();
+    const uint64_t Bl = nBl, Glm = nGl;
+    if (i + nwarps < n) {
+      stage_copy(nxt, J, cb, i + nwarps, J.stage_elems, lane);
+      nBl = __ldg(ltab + (size_t)(i + nwarps) * J.rec_elems);
+      nGl = __ldg(ltab + (size_t)(i + nwarps) * J.rec_elems + 32);
+    } else {
+      stage_commit_empty();
+    }
     stage_wait_prev();
     __syncwarp();
     const uint32_t nact = (uint32_t)cur[kElNact];
@@ -540,47 +575,86 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       // they multiply stay in Montgomery form, so products stay comparable.
       const uint64_t Bw = cur[kElBw], Bq = cur[kElBq], B2w = cur[kElB2w], B2q = cur[kElB2q];
       const uint64_t Gw = cur[kElGw], Gq = cur[kElGq];
-      const uint64_t Glm = cur[kElG + lane];
-      const uint64_t Glw = montmul(Glm, 1, p, pinv), Glq = shoup_const(Glm, pinv);
-      const uint64_t Bl = cur[kElB + lane];
+      const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
       const uint64_t Bl32 = shoup_mul(Bl, Bw, Bq, p);  // B^(lane+32)
       // clear the table (tags and counts)
       const uint4 z4 = make_uint4(0, 0, 0, 0);
-      for (uint32_t q = lane; q < NB; q += 32) W.tab4[q] = z4;
+#pragma unroll 4
+      for (uint32_t q = lane; q < NB + NB / 4; q += 32) W.tab4[q] = z4;
       if (lane == 0) *ML.count = 0;
       __syncwarp();
 
       // Baby steps: chain A owns j = lane + 64t, chain B j = lane + 32 + 64t.
+      // Values whose home bucket is full go to a short list (the match list's
+      // space, unused until the giant steps) and are inserted after the loop.
+      uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
       {
         uint64_t va = Bl, vb = Bl32;
         const uint32_t nfull = J.m / 64;  // iterations where every lane inserts twice
-#pragma unroll 1
+#pragma unroll 2
         for (uint32_t t = 0; t < nfull; t++) {
-          W.insert(va);
-          W.insert(vb);
+          const bool fa = W.insert_home(va);
+          const bool fb = W.insert_home(vb);
+          if (!(fa && fb)) {
+            if (!fa) ML.append(ovf, va);
+            if (!fb) ML.append(ovf, vb);
+          }
           va = shoup_mul(va, B2w, B2q, p);
           vb = shoup_mul(vb, B2w, B2q, p);
         }
         const uint32_t ja = lane + 64 * nfull;
-        if (ja < J.m) W.insert(va);
-        if (ja + 32 < J.m) W.insert(vb);
+        if (ja < J.m && !W.insert_home(va)) ML.append(ovf, va);
+        if (ja + 32 < J.m && !W.insert_home(vb)) ML.append(ovf, vb);
       }
       __syncwarp();
+      const uint32_t novf = *ML.count;
+      if (novf > (uint32_t)kOvfCap) {  // pathological table: leave the prime to the exact path
+        if (lane == 0) {
+          const uint32_t r = atomicAdd(cb.redo_count, 1u);
+          if (r < cb.cap) cb.redo[r] = i;
+        }
+        __syncwarp();
+        continue;
+      }
+      if (novf) {
+        const uint64_t v = lane < novf ? ovf[lane] : 0;
+        __syncwarp();
+        if (lane == 0) *ML.count = 0;
+        if (lane < novf) W.insert_after((uint32_t)v, (uint32_t)v & W.bmask);
+        __syncwarp();
+      }
 
       // Giant steps: lane (lane_row, lane_t) takes row slots g*RPI + lane_row for
       // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
       const uint32_t ngi = (nact + RPI - 1) / RPI;
       const uint64_t *Vs = J.stage_full ? cur + kElV : cb.recs + (size_t)i * J.rec_elems + kElV;
-      if (spl == 1) {
-#pragma unroll 1
+      if (spl == 1 && ngi <= 64) {
+        // One giant step per slot.  The loop only tests each value's home
+        // bucket and collects the outcome as bits (pass gi of chain A or B ->
+        // bit gi/2); tag hits and full home buckets are finished after it.
+        uint32_t hA = 0, hB = 0;
+#pragma unroll 2
         for (uint32_t gi = 0; gi < ngi; gi += 2) {
           const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
           const uint64_t ya = shoup_mul(Vs[min(sa, nact - 1)], Glw, Glq, p);
           const uint64_t yb = shoup_mul(Vs[min(sb, nact - 1)], Glw, Glq, p);
-          const bool ha = W.probe(ya) && sa < nact;
-          const bool hb = W.probe(yb) && sb < nact;
-          if (ha) ML.push(ya, sa, lane_t + 1);
-          if (hb) ML.push(yb, sb, lane_t + 1);
+          hA |= (uint32_t)W.probe_home(ya) << (gi >> 1);
+          hB |= (uint32_t)W.probe_home(yb) << (gi >> 1);
+        }
+        if (hA | hB) {
+#pragma unroll 1
+          for (uint32_t h = 0; h < 2; h++) {
+            uint32_t bits = h ? hB : hA;
+            while (bits) {
+              const uint32_t g = 2 * (__ffs(bits) - 1) + h;
+              bits &= bits - 1;
+              const uint32_t sl = g * RPI + lane_row;
+              if (sl < nact) {
+                const uint64_t y = shoup_mul(Vs[sl], Glw, Glq, p);
+                if (W.probe(y)) ML.push(y, sl, lane_t + 1);
+              }
+            }
+          }
         }
       } else {
 #pragma unroll 1
@@ -623,8 +697,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
               for (uint32_t q = 0; q < mc; q++) {
                 const Match mt = ML.list[q];
                 if (mt.y == v) {
-                  const uint64_t pk = J.stage_full ? cur[J.el_row + (mt.slot >> 2)]
-                                                   : rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                  const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
                   record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s, j);
                 }
               }
@@ -681,7 +754,7 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     const uint64_t Bs = rec_el(J, cb, kElBs, i), Gs = rec_el(J, cb, kElGs, i);
     for (uint32_t q = lane; q < S; q += 32) tab[q] = kEmpty;
     __syncwarp();
-    uint64_t v = rec_el(J, cb, kElB + lane, i);
+    uint64_t v = rec_el(J, cb, J.el_tab + lane, i);
 #pragma unroll 1
     for (uint32_t j = lane; j < J.m; j += 32) {
       uint32_t h = (uint32_t)v & tmask;
@@ -694,7 +767,7 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       v = montmul(v, Bs, p, pinv);
     }
     __syncwarp();
-    const uint64_t Gl = rec_el(J, cb, kElG + lane, i);
+    const uint64_t Gl = rec_el(J, cb, J.el_tab + 32 + lane, i);
     const uint32_t ngi = (nact + J.rows_per_it - 1) / J.rows_per_it;
 #pragma unroll 1
     for (uint32_t gi = 0; gi < ngi; gi++) {
