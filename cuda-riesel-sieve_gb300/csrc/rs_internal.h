@@ -11,7 +11,7 @@ namespace rs {
 // BSGS fast path: per-prime hash of 16-bit tags, kBucket tags per 16-byte bucket.
 constexpr uint32_t kEmptyTag = 0xffffu;
 constexpr int kBucket = 8;
-constexpr int kMatchCap = 16;       // deferred tag matches per prime before the exact path
+constexpr int kMatchCap = 15;       // deferred tag matches per prime before the exact path
 // BSGS exact path (rare primes): 32-bit entries (tag << jbits) | j, linear probing.
 // j <= m-1 <= 2^jbits - 2, so a real entry is never all ones.
 constexpr uint32_t kEmpty = 0xffffffffu;

@@ -182,20 +182,52 @@ __device__ __forceinline__ void rec_st2(uint64_t *rec, uint32_t e, uint64_t a, u
 }
 
 constexpr uint32_t kSetupRegQ = 8;  // Q up to this keeps the table of b^r*B^e0 in shared memory
+constexpr uint32_t kTabChunks = 8;  // 16-byte value pairs per lane per staging round
+constexpr uint32_t kTabPad = 33;    // chunk slots per staging row: 32 lanes + 1, so column reads are conflict-free
 
+// Per-warp shared memory of the setup kernel: first the staging area of the
+// lane tables, then (reused) the per-thread table of b^r*B^e0 and its Shoup
+// constants.
+union SetupWarpSmem {
+  uint4 stage[kTabChunks][kTabPad];
+  uint64_t hb[kSetupRegQ][2][32];
+};
+
+// Writes 16 consecutive table values of each of the warp's 32 records, starting
+// at element e0: every lane has put its values (as pairs, chunk c = values 2c,
+// 2c+1) into column `lane` of the staging area; the warp then stores whole
+// record runs of 128 bytes (four records per instruction) instead of 32
+// scattered 16-byte pieces.
+__device__ __forceinline__ void flush_table_round(const SetupWarpSmem &S, uint64_t *recs, uint32_t rec_elems,
+                                                  uint32_t i0, uint32_t n, uint32_t e0, uint32_t lane) {
+  __syncwarp();
+  const uint32_t c = lane & (kTabChunks - 1);
+#pragma unroll
+  for (uint32_t q = 0; q < 32; q += 32 / kTabChunks) {
+    const uint32_t r = q + lane / kTabChunks;
+    const uint4 v = S.stage[c][r];
+    if (i0 + r < n) *reinterpret_cast<uint4 *>(recs + (size_t)(i0 + r) * rec_elems + e0 + 2 * c) = v;
+  }
+  __syncwarp();
+}
+
+// One thread per prime (a warp per 32 consecutive primes).  Lanes past the
+// chunk's prime count compute on a stand-in prime and store nothing.
 __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ SetupWarpSmem smem[4];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  SetupWarpSmem &S = smem[warp];
+  const uint32_t i0 = blockIdx.x * blockDim.x + warp * 32;
+  const uint32_t i = i0 + lane;
   const uint32_t cnt = *cb.count;
   const uint32_t n = cnt < cb.cap ? cnt : cb.cap;
-  if (i >= n) return;
-  const uint64_t p = cb.primes[i];
+  if (i0 >= n) return;  // the whole warp
+  const bool live = i < n;
+  const uint64_t p = live ? cb.primes[i] : 1000000007ull;
   uint64_t *rec = cb.recs + (size_t)i * J.rec_elems;
-  const uint64_t bmod = p > J.base ? (uint64_t)J.base : (uint64_t)J.base % p;
-  if (bmod == 0) {  // p | b: no k*b^n+-1 is divisible by p
-    rec_st2(rec, kElP, p, 0);
-    rec_st2(rec, kElNact, 0, 0);
-    return;
-  }
+  const uint64_t b0 = p > J.base ? (uint64_t)J.base : (uint64_t)J.base % p;
+  const bool pb = b0 == 0;          // p | b: no k*b^n+-1 is divisible by p (nact = 0)
+  const uint64_t bmod = pb ? 1 : b0;  // keeps the arithmetic below defined
   Mont M;
   M.p = p;
   M.pinv = mont_pinv(p);
@@ -209,46 +241,62 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const uint64_t G = mont_pow(B, J.m, one, M);     // B^m
 
   // Lane tables: B^lane (baby starts) and G^(lane % tlanes + 1) (giant multipliers),
-  // stepped with Shoup products by the fixed B and G.
+  // stepped with Shoup products by the fixed B and G, 16 values per round.
   uint64_t Bs, Gs = 0;
   {
     const uint64_t Bw = from_mont(B, p, M.pinv), Bq = shoup_const(B, M.pinv);
     uint64_t v = one;
+#pragma unroll 1
+    for (uint32_t h = 0; h < 2; h++) {
 #pragma unroll 4
-    for (uint32_t l = 0; l < 32; l += 2) {
-      const uint64_t v1 = shoup_mul(v, Bw, Bq, p);
-      rec_st2(rec, J.el_tab + l, v, v1);
-      v = shoup_mul(v1, Bw, Bq, p);
+      for (uint32_t c = 0; c < kTabChunks; c++) {
+        const uint64_t v1 = shoup_mul(v, Bw, Bq, p);
+        S.stage[c][lane] = make_uint4((uint32_t)v, (uint32_t)(v >> 32), (uint32_t)v1, (uint32_t)(v1 >> 32));
+        v = shoup_mul(v1, Bw, Bq, p);
+      }
+      flush_table_round(S, cb.recs, J.rec_elems, i0, n, J.el_tab + 16 * h, lane);
     }
     Bs = v;  // B^32
+    // value t of the G table is G^(t % tlanes + 1): the chain restarts at G
+    // whenever t % tlanes wraps to 0 (tlanes divides 32)
     const uint64_t Gw = from_mont(G, p, M.pinv), Gq = shoup_const(G, M.pinv);
-    if (J.tlanes == 1) {
+    uint64_t g = G;
+    uint32_t k = 0;
 #pragma unroll 1
-      for (uint32_t l = 0; l < 32; l += 2) rec_st2(rec, J.el_tab + 32 + l, G, G);
-    } else {
-      uint64_t g = G;
+    for (uint32_t h = 0; h < 2; h++) {
 #pragma unroll 1
-      for (uint32_t l = 0; l < J.tlanes; l += 2) {
-        const uint64_t g1 = shoup_mul(g, Gw, Gq, p);
-#pragma unroll 1
-        for (uint32_t c = l; c < 32; c += J.tlanes) rec_st2(rec, J.el_tab + 32 + c, g, g1);
-        if (l == 30) Gs = g1;  // G^32
-        g = shoup_mul(g1, Gw, Gq, p);
+      for (uint32_t c = 0; c < kTabChunks; c++) {
+        uint64_t pair[2];
+#pragma unroll
+        for (uint32_t u = 0; u < 2; u++) {
+          pair[u] = g;
+          if (++k == J.tlanes) {
+            k = 0;
+            g = G;
+          } else {
+            g = shoup_mul(g, Gw, Gq, p);
+          }
+        }
+        S.stage[c][lane] =
+            make_uint4((uint32_t)pair[0], (uint32_t)(pair[0] >> 32), (uint32_t)pair[1], (uint32_t)(pair[1] >> 32));
+        if (h == 1 && c == kTabChunks - 1) Gs = pair[1];  // G^32 when tlanes == 32
       }
+      flush_table_round(S, cb.recs, J.rec_elems, i0, n, J.el_tab + 32 + 16 * h, lane);
     }
+    if (J.tlanes != 32) Gs = 0;
   }
 
   // HB[r] = b^r * B^e0 (Montgomery form) with the Shoup constant of HB[r] taken
   // as an integer, so the start value of row (k, r) is the single product k*HB[r].
-  // Kept per thread in shared memory (indexed by r without a select chain).
-  __shared__ uint64_t hb_sm[kSetupRegQ][2][128];
+  // Kept per thread in shared memory (indexed by r without a select chain); the
+  // staging area is free again after the last flush.
   const bool regtab = J.Q <= kSetupRegQ;
   if (regtab) {
     uint64_t h = H;
 #pragma unroll 1
     for (uint32_t r = 0; r < J.Q; r++) {
-      hb_sm[r][0][threadIdx.x] = h;
-      hb_sm[r][1][threadIdx.x] = shoup_const(montmul(h, r2, M), M.pinv);
+      S.hb[r][0][lane] = h;
+      S.hb[r][1][lane] = shoup_const(montmul(h, r2, M), M.pinv);
       h = shoup_mul(h, bmod, bq, p);
     }
   }
@@ -262,17 +310,19 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   uint64_t vprev = 0, rp0 = 0, rp1 = 0;
 #pragma unroll 1
   for (uint32_t c0 = 0; c0 < J.nk; c0 += 4) {
-    // the four characters first, so their table loads are in flight together
-    int ch[4];
+    // the four characters first, so their table loads are in flight together;
+    // kept as 2-bit fields (character + 1) so that no array goes to local memory
+    uint32_t chpack = 0;
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (uint32_t u = 0; u < 4; u++) {
       const uint32_t c = c0 + u;
-      ch[u] = c < J.nk ? legendre_k_tab(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c], J.k_jac[c], J.jac_bits) : 0;
+      const int ch = c < J.nk ? legendre_k_tab(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c], J.k_jac[c], J.jac_bits) : 0;
+      chpack |= (uint32_t)(ch + 1) << (2 * u);
     }
 #pragma unroll 1
-    for (int u = 0; u < 4; u++) {
+    for (uint32_t u = 0; u < 4; u++) {
       const uint32_t c = c0 + u;
-      int chik = ch[u];
+      int chik = (int)((chpack >> (2 * u)) & 3u) - 1;
       if (c >= J.nk) break;
       if (J.sign > 0) chik *= chim1;  // character of -k
       if (chik == 0) continue;        // p | k
@@ -288,7 +338,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
         const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
         if (!act) continue;
         if (regtab) {
-          V = shoup_mul(kx, hb_sm[r][0][threadIdx.x], hb_sm[r][1][threadIdx.x], p);
+          V = shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p);
         } else {
           if (!have) {
             V = montmul(montmul(kx, r2, M), H, M);
@@ -297,24 +347,28 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
 #pragma unroll 1
           for (; cur < r; cur++) V = shoup_mul(V, bmod, bq, p);
         }
-        if (nact & 1) rec_st2(rec, kElV + nact - 1, vprev, V);
-        else vprev = V;
+        if (nact & 1) {
+          if (live) rec_st2(rec, kElV + nact - 1, vprev, V);
+        } else {
+          vprev = V;
+        }
         const uint64_t rbits = (uint64_t)row << (16 * (nact & 3));
         if (nact & 4) rp1 |= rbits;
         else rp0 |= rbits;
         if ((nact & 7) == 7) {
-          rec_st2(rec, J.el_row + (nact >> 2) - 1, rp0, rp1);
+          if (live) rec_st2(rec, J.el_row + (nact >> 2) - 1, rp0, rp1);
           rp0 = rp1 = 0;
         }
         nact++;
       }
     }
   }
+  if (!live) return;
   if (nact & 1) rec[kElV + nact - 1] = vprev;
   if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBs, Bs, Gs);
-  rec_st2(rec, kElNact, nact, 0);
+  rec_st2(rec, kElNact, pb ? 0 : nact, 0);
   {
     // the strides in normal form with their Shoup constants, once per prime
     const uint64_t B2 = montmul(Bs, Bs, M);  // B^64
@@ -591,7 +645,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       {
         uint64_t va = Bl, vb = Bl32;
         const uint32_t nfull = J.m / 64;  // iterations where every lane inserts twice
-#pragma unroll 2
+#pragma unroll 4
         for (uint32_t t = 0; t < nfull; t++) {
           const bool fa = W.insert_home(va);
           const bool fb = W.insert_home(vb);
