@@ -689,11 +689,24 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         uint32_t hA = 0, hB = 0;
 #pragma unroll 2
         for (uint32_t gi = 0; gi < ngi; gi += 2) {
-          const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
-          const uint64_t ya = shoup_mul(Vs[min(sa, nact - 1)], Glw, Glq, p);
-          const uint64_t yb = shoup_mul(Vs[min(sb, nact - 1)], Glw, Glq, p);
-          hA |= (uint32_t)W.probe_home(ya) << (gi >> 1);
-          hB |= (uint32_t)W.probe_home(yb) << (gi >> 1);
+          uint64_t va, vb;
+          if (RPI == 1) {
+            // slots gi, gi+1 are adjacent: one 16-byte load (gi even, V 16-byte
+            // aligned).  Slot gi+1 may be past nact; its value (still inside the
+            // V area) is discarded after the loop.
+            const uint4 w = *reinterpret_cast<const uint4 *>(Vs + gi);
+            va = ((uint64_t)w.y << 32) | w.x;
+            vb = ((uint64_t)w.w << 32) | w.z;
+          } else {
+            const uint32_t sa = gi * RPI + lane_row;
+            va = Vs[min(sa, nact - 1)];
+            vb = Vs[min(sa + RPI, nact - 1)];
+          }
+          const uint64_t ya = shoup_mul(va, Glw, Glq, p);
+          const uint64_t yb = shoup_mul(vb, Glw, Glq, p);
+          const uint32_t bit = 1u << (gi >> 1);
+          if (W.probe_home(ya)) hA |= bit;
+          if (W.probe_home(yb)) hB |= bit;
         }
         if (hA | hB) {
 #pragma unroll 1
