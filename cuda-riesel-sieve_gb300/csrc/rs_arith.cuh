@@ -55,6 +55,24 @@ __device__ __forceinline__ uint64_t shoup_mul(uint64_t x, uint64_t w, uint64_t w
   return (int64_t)t < 0 ? r : t;
 }
 
+// x*c mod p for a small integer multiplier c, with rc = floor(2^64 / p).
+// Requires x < p, 2^33 < p and c*p < 2^63.  Then P = x*c < 2^63 and the
+// quotient estimate q' = floor(hi32(P) * rc / 2^32) satisfies
+//   P/p - 1 - (hi32(P)/2^32 + 2^32/p) < q' <= P/p,
+// where the bracket is below 1/2 + 1/2, so q' is floor(P/p) or one less and
+// r = P - q'*p lies in [0, 2p): one masked subtraction finishes.  Two 32x32
+// products form P, one high product forms q', and one multiply-add forms r,
+// against ten multiplies for Shoup's product by a full-size constant.  The
+// product of a Montgomery-form x by an integer is the Montgomery form of the
+// product, so x may be in either form.
+__device__ __forceinline__ uint64_t mul_small(uint64_t x, uint32_t c, uint32_t rc, uint64_t p) {
+  const uint64_t P = x * (uint64_t)c;
+  const uint32_t q = __umulhi((uint32_t)(P >> 32), rc);
+  const uint64_t r = P + (uint64_t)q * (0 - p);
+  const uint64_t t = r - p;
+  return (int64_t)t < 0 ? r : t;
+}
+
 // floor(w * 2^64 / p) from the Montgomery form wm = w * 2^64 mod p: since
 // w * 2^64 = wq * p + wm, wq == -wm * p^-1 == wm * pinv (mod 2^64), and
 // wq < 2^64 because w < p.  One 64-bit multiply instead of a 128/64 division.

@@ -234,7 +234,9 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
     const double ER = rows * ((Q & 1) ? 0.75 : 0.5);
     for (uint32_t tl = 0; tl <= 20; tl++) {
       const uint64_t T = (uint64_t)1 << tl;
-      const uint64_t m = (X + T - 1) / T;
+      uint64_t m = (X + T - 1) / T;
+      // whole baby chains (64 chains of equal length) when that stays within the cap
+      if (m > 64 && ((m + 63) & ~63ull) <= mcap) m = (m + 63) & ~63ull;
       if (m > mcap) continue;
       if (m * T < X) continue;
       const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));  // exact-path table
@@ -428,6 +430,12 @@ static int upload_job(rs_job *j) {
   d.sign = s.sign;
   d.Q = pl.Q;
   d.m = pl.m;
+  d.chain_len = (pl.m + 63) / 64;
+  {
+    uint64_t bq = 1;
+    for (uint32_t q = 0; q < pl.Q && bq; q++) bq = (bq * s.base < (1ull << 32)) ? bq * s.base : 0;
+    d.bq_small = (uint32_t)bq;
+  }
   d.T = pl.T;
   d.tlanes = pl.tlanes;
   d.rows_per_it = pl.rows_per_it;
@@ -822,6 +830,12 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
+      {
+        // short baby-step products need p > 2^33 and b^Q * p < 2^63 for every p of the chunk
+        const uint64_t bq = j->dev.bq_small;
+        j->cb.small_step = bq != 0 && todo[c].a > (1ull << 33) &&
+                           (unsigned __int128)bq * todo[c].b < ((unsigned __int128)1 << 63);
+      }
       if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
       if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 3], j->st);

@@ -24,15 +24,20 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // rec_elems (even) 64-bit elements per prime, contiguous, element e of prime i
 // at recs[i * rec_elems + e].  The BSGS kernel stages the header and V (the
 // first el_row elements) into shared memory with 16-byte cp.async copies and
-// loads each lane's own table entries straight into registers.  Element map:
-//   0 p, 1 pinv, 2 B^32 (baby stride), 3 G^32 (giant stride), 4 nact,
-//   6,7 B^64 in normal form and its Shoup constant, 8,9 B^32 likewise,
-//   10,11 G^32 likewise, 12.. V[max_act] (giant-step start per active row),
-//   el_row.. row ids (u16, 4 per element), el_tab.. B^lane (32 elements),
+// loads each lane's own table entries straight into registers.
+//
+// Baby steps run in 64 chains of chain_len consecutive exponents: chain c
+// covers j = c*chain_len + t, each step a product by B = b^Q.  Lane l owns
+// chains l and l + 32.  Element map:
+//   0 p, 1 pinv, 2 B, 3 G^32 (giant stride), 4 nact, 5 floor(2^64 / p),
+//   6,7 B in normal form and its Shoup constant (the chain step),
+//   8,9 B^(32*chain_len) likewise (chain l -> chain l+32), 10,11 G^32 likewise,
+//   12.. V[max_act] (giant-step start per active row), el_row.. row ids (u16,
+//   4 per element), el_tab.. B^(lane*chain_len) (32 elements, the chain starts),
 //   el_tab+32.. G^(lane % tlanes + 1) (32 elements).
 // Residues are in Montgomery form unless marked normal.
-constexpr uint32_t kElP = 0, kElPinv = 1, kElBs = 2, kElGs = 3, kElNact = 4;
-constexpr uint32_t kElB2w = 6, kElB2q = 7, kElBw = 8, kElBq = 9, kElGw = 10, kElGq = 11;
+constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kElRcp = 5;
+constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
 constexpr uint32_t kElV = 12;
 
 // Job constants, passed by value to every kernel (lives in the constant bank).
@@ -41,6 +46,8 @@ struct JobDev {
   int32_t sign;          // -1 Riesel, +1 Sierpinski
   uint32_t Q;
   uint32_t m;            // baby steps per prime
+  uint32_t chain_len;    // baby steps per chain, ceil(m / 64)
+  uint32_t bq_small;     // b^Q as an integer when below 2^32, else 0
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes
@@ -91,6 +98,9 @@ struct ChunkBufs {
   uint32_t *redo;       // [cap] primes handed to the exact BSGS kernel
   uint32_t *redo_count; // [1]
   uint32_t cap;
+  // 1 if every prime p of the chunk has p > 2^33 and b^Q * p < 2^63, so that a
+  // baby step is the short product by the small integer b^Q (mul_small)
+  uint32_t small_step;
 };
 
 struct HitBufs {

@@ -239,12 +239,14 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const uint64_t e = J.e0 >= 0 ? (uint64_t)J.e0 : (p - 1) - (uint64_t)(-J.e0) % (p - 1);
   const uint64_t H = mont_pow(B, e, one, M);       // B^e0
   const uint64_t G = mont_pow(B, J.m, one, M);     // B^m
+  const uint64_t Bc = mont_pow(B, J.chain_len, one, M);  // B^chain_len
 
-  // Lane tables: B^lane (baby starts) and G^(lane % tlanes + 1) (giant multipliers),
-  // stepped with Shoup products by the fixed B and G, 16 values per round.
+  // Lane tables: B^(lane*chain_len) (baby chain starts) and G^(lane % tlanes + 1)
+  // (giant multipliers), stepped with Shoup products by the fixed B^chain_len
+  // and G, 16 values per round.
   uint64_t Bs, Gs = 0;
   {
-    const uint64_t Bw = from_mont(B, p, M.pinv), Bq = shoup_const(B, M.pinv);
+    const uint64_t Bw = from_mont(Bc, p, M.pinv), Bq = shoup_const(Bc, M.pinv);
     uint64_t v = one;
 #pragma unroll 1
     for (uint32_t h = 0; h < 2; h++) {
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
       }
       flush_table_round(S, cb.recs, J.rec_elems, i0, n, J.el_tab + 16 * h, lane);
     }
-    Bs = v;  // B^32
+    Bs = v;  // B^(32*chain_len)
     // value t of the G table is G^(t % tlanes + 1): the chain restarts at G
     // whenever t % tlanes wraps to 0 (tlanes divides 32)
     const uint64_t Gw = from_mont(G, p, M.pinv), Gq = shoup_const(G, M.pinv);
@@ -367,15 +369,13 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   if (nact & 1) rec[kElV + nact - 1] = vprev;
   if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
   rec_st2(rec, kElP, p, M.pinv);
-  rec_st2(rec, kElBs, Bs, Gs);
-  rec_st2(rec, kElNact, pb ? 0 : nact, 0);
-  {
-    // the strides in normal form with their Shoup constants, once per prime
-    const uint64_t B2 = montmul(Bs, Bs, M);  // B^64
-    rec_st2(rec, kElB2w, from_mont(B2, p, M.pinv), shoup_const(B2, M.pinv));
-    rec_st2(rec, kElBw, from_mont(Bs, p, M.pinv), shoup_const(Bs, M.pinv));
-    rec_st2(rec, kElGw, from_mont(Gs, p, M.pinv), shoup_const(Gs, M.pinv));
-  }
+  rec_st2(rec, kElBm, B, Gs);
+  // floor(2^64/p) is the Shoup constant of 1, whose Montgomery form is `one`
+  rec_st2(rec, kElNact, pb ? 0 : nact, shoup_const(one, M.pinv));
+  // the strides in normal form with their Shoup constants, once per prime
+  rec_st2(rec, kElStw, from_mont(B, p, M.pinv), shoup_const(B, M.pinv));
+  rec_st2(rec, kElOfw, from_mont(Bs, p, M.pinv), shoup_const(Bs, M.pinv));
+  rec_st2(rec, kElGw, from_mont(Gs, p, M.pinv), shoup_const(Gs, M.pinv));
 }
 
 // Quadratic-character tables: word w of the table of odd k' holds bit t =
@@ -561,6 +561,37 @@ struct MatchList {
   }
 };
 
+// One chain step: the product by B, as Shoup's product by the full-size
+// constant or, when the chunk allows it, as the short product by the integer b^Q.
+struct StepShoup {
+  uint64_t w, wq, p;
+  __device__ __forceinline__ uint64_t operator()(uint64_t x) const { return shoup_mul(x, w, wq, p); }
+};
+struct StepSmall {
+  uint32_t c, rc;
+  uint64_t p;
+  __device__ __forceinline__ uint64_t operator()(uint64_t x) const { return mul_small(x, c, rc, p); }
+};
+
+// Baby steps of one lane: two chains of `len` steps from va and vb, of which
+// the first na (nb) are inserted (all of them when FULL).  A value whose home bucket is full is
+// appended to ovf and inserted after the loop.
+template <bool FULL, class Step>
+__device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList &ML, uint64_t *ovf, uint64_t va,
+                                            uint64_t vb, uint32_t na, uint32_t nb, uint32_t len, const Step &step) {
+#pragma unroll 4
+  for (uint32_t t = 0; t < len; t++) {
+    const bool fa = (!FULL && t >= na) || W.insert_home(va);
+    const bool fb = (!FULL && t >= nb) || W.insert_home(vb);
+    if (!(fa && fb)) {
+      if (!fa) ML.append(ovf, va);
+      if (!fb) ML.append(ovf, vb);
+    }
+    va = step(va);
+    vb = step(vb);
+  }
+}
+
 // Per-warp shared memory of the fast kernel:
 //   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
 // The stages hold a record's header and V (double-buffered with cp.async); each
@@ -593,7 +624,6 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   const uint32_t n = total < cb.cap ? total : cb.cap;
   const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
   const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
-  const uint32_t nbaby2 = (J.m + 63) / 64;  // iterations of the two-chain baby loop
   const uint32_t spl = J.steps_per_lane;
   const uint64_t *ltab = cb.recs + J.el_tab + lane;  // this lane's B^lane; G^(lane+1) 32 further
 
@@ -627,10 +657,15 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       const uint64_t p = cur[kElP], pinv = cur[kElPinv];
       // Multipliers in normal form with their Shoup constants; the values
       // they multiply stay in Montgomery form, so products stay comparable.
-      const uint64_t Bw = cur[kElBw], Bq = cur[kElBq], B2w = cur[kElB2w], B2q = cur[kElB2q];
+      const uint64_t Stw = cur[kElStw], Stq = cur[kElStq];
       const uint64_t Gw = cur[kElGw], Gq = cur[kElGq];
       const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
-      const uint64_t Bl32 = shoup_mul(Bl, Bw, Bq, p);  // B^(lane+32)
+      // chain starts B^(lane*CL) and B^((lane+32)*CL); valid steps na, nb (j < m)
+      const uint32_t CL = J.chain_len;
+      const uint32_t ja0 = lane * CL, jb0 = ja0 + 32 * CL;
+      const uint32_t na = J.m > ja0 ? min(CL, J.m - ja0) : 0;
+      const uint32_t nb = J.m > jb0 ? min(CL, J.m - jb0) : 0;
+      const uint64_t Blb = shoup_mul(Bl, cur[kElOfw], cur[kElOfq], p);
       // clear the table (tags and counts)
       const uint4 z4 = make_uint4(0, 0, 0, 0);
 #pragma unroll 4
@@ -638,27 +673,20 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       if (lane == 0) *ML.count = 0;
       __syncwarp();
 
-      // Baby steps: chain A owns j = lane + 64t, chain B j = lane + 32 + 64t.
-      // Values whose home bucket is full go to a short list (the match list's
-      // space, unused until the giant steps) and are inserted after the loop.
+      // Baby steps: chain A owns j = ja0 + t, chain B j = jb0 + t.  Values whose
+      // home bucket is full go to a short list (the match list's space, unused
+      // until the giant steps) and are inserted after the loop.
       uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
-      {
-        uint64_t va = Bl, vb = Bl32;
-        const uint32_t nfull = J.m / 64;  // iterations where every lane inserts twice
-#pragma unroll 4
-        for (uint32_t t = 0; t < nfull; t++) {
-          const bool fa = W.insert_home(va);
-          const bool fb = W.insert_home(vb);
-          if (!(fa && fb)) {
-            if (!fa) ML.append(ovf, va);
-            if (!fb) ML.append(ovf, vb);
-          }
-          va = shoup_mul(va, B2w, B2q, p);
-          vb = shoup_mul(vb, B2w, B2q, p);
-        }
-        const uint32_t ja = lane + 64 * nfull;
-        if (ja < J.m && !W.insert_home(va)) ML.append(ovf, va);
-        if (ja + 32 < J.m && !W.insert_home(vb)) ML.append(ovf, vb);
+      if (J.m == 64 * CL) {  // every chain full (the planner's usual choice of m)
+        if (cb.small_step)
+          baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
+        else
+          baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
+      } else {
+        if (cb.small_step)
+          baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
+        else
+          baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
       }
       __syncwarp();
       const uint32_t novf = *ML.count;
@@ -752,26 +780,26 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
           if (r < cb.cap) cb.redo[r] = i;
         }
       } else if (mc > 0) {
-        uint64_t va = Bl, vb = Bl32;
+        uint64_t va = Bl, vb = Blb;
 #pragma unroll 1
-        for (uint32_t t = 0; t < nbaby2; t++) {
+        for (uint32_t t = 0; t < CL; t++) {
 #pragma unroll 1
           for (uint32_t h = 0; h < 2; h++) {
-            const uint32_t j = lane + 64 * t + 32 * h;
             const uint64_t v = h ? vb : va;
-            if (j < J.m) {
+            if (t < (h ? nb : na)) {
 #pragma unroll 1
               for (uint32_t q = 0; q < mc; q++) {
                 const Match mt = ML.list[q];
                 if (mt.y == v) {
                   const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
-                  record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s, j);
+                  record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s,
+                             (h ? jb0 : ja0) + t);
                 }
               }
             }
           }
-          va = shoup_mul(va, B2w, B2q, p);
-          vb = shoup_mul(vb, B2w, B2q, p);
+          va = shoup_mul(va, Stw, Stq, p);
+          vb = shoup_mul(vb, Stw, Stq, p);
         }
       }
     }
@@ -818,20 +846,27 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     const uint32_t i = cb.redo[r];
     const uint64_t p = rec_el(J, cb, kElP, i), pinv = rec_el(J, cb, kElPinv, i);
     const uint32_t nact = (uint32_t)rec_el(J, cb, kElNact, i);
-    const uint64_t Bs = rec_el(J, cb, kElBs, i), Gs = rec_el(J, cb, kElGs, i);
+    const uint64_t Gs = rec_el(J, cb, kElGs, i);
+    const uint64_t Stw = rec_el(J, cb, kElStw, i), Stq = rec_el(J, cb, kElStq, i);
     for (uint32_t q = lane; q < S; q += 32) tab[q] = kEmpty;
     __syncwarp();
-    uint64_t v = rec_el(J, cb, J.el_tab + lane, i);
+    // the lane's two baby chains, j = (lane + 32c)*chain_len + t
+    const uint64_t Bl = rec_el(J, cb, J.el_tab + lane, i);
 #pragma unroll 1
-    for (uint32_t j = lane; j < J.m; j += 32) {
-      uint32_t h = (uint32_t)v & tmask;
-      const uint32_t e = ((((uint32_t)(v >> tl)) & tagmask) << jbits) | j;
+    for (uint32_t c = 0; c < 2; c++) {
+      const uint32_t j0 = (lane + 32 * c) * J.chain_len;
+      uint64_t v = c ? shoup_mul(Bl, rec_el(J, cb, kElOfw, i), rec_el(J, cb, kElOfq, i), p) : Bl;
 #pragma unroll 1
-      for (uint32_t t = 0; t < S; t++) {
-        if (atomicCAS(&tab[h], kEmpty, e) == kEmpty) break;
-        h = (h + 1) & tmask;
+      for (uint32_t j = j0; j < J.m && j < j0 + J.chain_len; j++) {
+        uint32_t h = (uint32_t)v & tmask;
+        const uint32_t e = ((((uint32_t)(v >> tl)) & tagmask) << jbits) | j;
+#pragma unroll 1
+        for (uint32_t t = 0; t < S; t++) {
+          if (atomicCAS(&tab[h], kEmpty, e) == kEmpty) break;
+          h = (h + 1) & tmask;
+        }
+        v = shoup_mul(v, Stw, Stq, p);
       }
-      v = montmul(v, Bs, p, pinv);
     }
     __syncwarp();
     const uint64_t Gl = rec_el(J, cb, J.el_tab + 32 + lane, i);
