@@ -463,14 +463,20 @@ struct __align__(16) Match {
 };
 
 // 16-bit tag of a residue: the high half of its low word (the bucket index
-// uses the low log2(NB) <= 16 bits), never 0 (0 marks an empty slot).
-__device__ __forceinline__ uint32_t tag16(uint32_t lo) { return max(lo >> 16, 1u); }
+// uses the low log2(NB) <= 16 bits), raised to 1 if 0 (0 marks an empty slot).
+// tag_pair gives it in both halves, t*0x10001: the high half copied to both
+// halves, each raised to at least 1; its low half is the tag itself.
+__device__ __forceinline__ uint32_t tag_pair(uint32_t lo) { return __vmaxu2(__byte_perm(lo, 0, 0x3232), 0x00010001u); }
+
+// Nonzero iff some 16-bit half of x is zero: (x - 0x10001) & ~x sets bit 15 of
+// the low half iff it is zero, and bit 15 of the high half iff it is zero or
+// the low half borrowed (which only happens when the low half is zero).
+__device__ __forceinline__ uint32_t zero_half(uint32_t x) { return (x - 0x00010001u) & ~x & 0x80008000u; }
 
 // Bucket layout: 16 bytes = eight 16-bit tags (0 = empty).  True iff one of
 // the 8 tags equals the tag pair T = t*0x10001.
 __device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
-  const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
-  return (m & 0xffffu) == 0 || m < 0x10000u;
+  return zero_half(__vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T))) != 0;
 }
 
 constexpr uint32_t kSlots = 8;  // tag slots per bucket
@@ -500,7 +506,7 @@ struct WarpTable {
       b = (b + 1) & bmask;
       c = take(b);
     }
-    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag16(lo);
+    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
   }
 
   // Insert into the home bucket; false if it was full (the caller finishes the
@@ -509,7 +515,7 @@ struct WarpTable {
     const uint32_t lo = (uint32_t)v;
     const uint32_t b = lo & bmask;
     const uint32_t c = take(b);
-    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag16(lo);
+    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
     return c < kSlots;
   }
 
@@ -518,14 +524,16 @@ struct WarpTable {
   __device__ __forceinline__ bool probe_home(uint64_t y) const {
     const uint32_t lo = (uint32_t)y;
     const uint4 q = tab4[lo & bmask];
-    return bucket_has(q, tag16(lo) * 0x10001u) || q.w >= 0x10000u;
+    const uint32_t T = tag_pair(lo);
+    const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
+    return (zero_half(m) | (q.w & 0xffff0000u)) != 0;  // a tag match, or slot 7 taken
   }
 
   // True iff some entry with the tag of y lies in y's probe sequence.
   __device__ __forceinline__ bool probe(uint64_t y) const {
     const uint32_t lo = (uint32_t)y;
     uint32_t b = lo & bmask;
-    const uint32_t T = tag16(lo) * 0x10001u;
+    const uint32_t T = tag_pair(lo);
     uint4 q = tab4[b];
     bool hit = bucket_has(q, T);
     if (q.w >= 0x10000u) {  // the home bucket is full, continue scanning
@@ -589,6 +597,36 @@ __device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList 
     }
     va = step(va);
     vb = step(vb);
+  }
+}
+
+// Giant steps with one step per row slot: lane (lane_row) multiplies the V of
+// slots gi*RPI + lane_row and (gi+1)*RPI + lane_row by its G^(lane_t+1) and
+// tests the home buckets; bit gi/2 of hA (hB) records a hit or full bucket.
+template <uint32_t RPI>
+__device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *__restrict__ Vs, uint32_t ngi,
+                                           uint32_t nact, uint32_t lane_row, uint64_t Glw, uint64_t Glq, uint64_t p,
+                                           uint32_t &hA, uint32_t &hB) {
+#pragma unroll 2
+  for (uint32_t gi = 0; gi < ngi; gi += 2) {
+    uint64_t va, vb;
+    if (RPI == 1) {
+      // slots gi, gi+1 are adjacent: one 16-byte load (gi even, V 16-byte
+      // aligned).  Slot gi+1 may be past nact; its value (still inside the V
+      // area) is discarded after the loop.
+      const uint4 w = *reinterpret_cast<const uint4 *>(Vs + gi);
+      va = ((uint64_t)w.y << 32) | w.x;
+      vb = ((uint64_t)w.w << 32) | w.z;
+    } else {
+      const uint32_t sa = gi * RPI + lane_row;
+      va = Vs[min(sa, nact - 1)];
+      vb = Vs[min(sa + RPI, nact - 1)];
+    }
+    const uint64_t ya = shoup_mul(va, Glw, Glq, p);
+    const uint64_t yb = shoup_mul(vb, Glw, Glq, p);
+    const uint32_t bit = 1u << (gi >> 1);
+    if (W.probe_home(ya)) hA |= bit;
+    if (W.probe_home(yb)) hB |= bit;
   }
 }
 
@@ -714,28 +752,13 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         // One giant step per slot.  The loop only tests each value's home
         // bucket and collects the outcome as bits (pass gi of chain A or B ->
         // bit gi/2); tag hits and full home buckets are finished after it.
+        // Separate calls for staged and global V keep each load's address
+        // space known to the compiler.
         uint32_t hA = 0, hB = 0;
-#pragma unroll 2
-        for (uint32_t gi = 0; gi < ngi; gi += 2) {
-          uint64_t va, vb;
-          if (RPI == 1) {
-            // slots gi, gi+1 are adjacent: one 16-byte load (gi even, V 16-byte
-            // aligned).  Slot gi+1 may be past nact; its value (still inside the
-            // V area) is discarded after the loop.
-            const uint4 w = *reinterpret_cast<const uint4 *>(Vs + gi);
-            va = ((uint64_t)w.y << 32) | w.x;
-            vb = ((uint64_t)w.w << 32) | w.z;
-          } else {
-            const uint32_t sa = gi * RPI + lane_row;
-            va = Vs[min(sa, nact - 1)];
-            vb = Vs[min(sa + RPI, nact - 1)];
-          }
-          const uint64_t ya = shoup_mul(va, Glw, Glq, p);
-          const uint64_t yb = shoup_mul(vb, Glw, Glq, p);
-          const uint32_t bit = 1u << (gi >> 1);
-          if (W.probe_home(ya)) hA |= bit;
-          if (W.probe_home(yb)) hB |= bit;
-        }
+        if (J.stage_full)
+          giant_home<RPI>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+        else
+          giant_home<RPI>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         if (hA | hB) {
 #pragma unroll 1
           for (uint32_t h = 0; h < 2; h++) {
