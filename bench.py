@@ -17,6 +17,8 @@ Extra keys: roofline (the BSGS kernel against this GPU's measured integer
 multiply throughput), cpu_baseline (the CPU oracle on a bounded sub-window),
 clocks (nvidia-smi sampled during the timed region), gpu_launches.
 
+--served runs the batched and served forms instead (see run_served).
+
 --impl reference times the reference's CPU path for the same metric.  The
 reference sieve (kernel_v0.24.6.cu) has no CPU implementation, so this arm runs
 the project's scalar CPU oracle (oracle/), all host cores, a bounded
@@ -231,6 +233,112 @@ def run_reference(args, rank: int) -> None:
     }))
 
 
+def run_served(args) -> None:
+    """--served: the batched and served forms on the mixed-job stream.
+
+    Jobs are drawn from the mixed-batch distribution (rsieve/synth.py
+    batch_job: base in [2, 1024] without perfect powers, 1-1000 k, n windows
+    of 1e4-2e6 at 1-10%, a p-window starting uniform in [1e12, 2^60]).  Three
+    runs over the same jobs: plain (one job after another through
+    rs_job_create_abcd + rs_sieve_range), batched (all submitted to an
+    rs_server at once) and served (Poisson arrivals at a sweep of loads,
+    relative to the batched capacity).  Every job's factors in the batched and
+    served runs are checked equal to its plain run.  Latencies are the
+    server's own submit-to-finish times.
+    """
+    import threading
+
+    import numpy as np
+
+    import rsieve
+    import rsieve.synth as S
+
+    rsieve.build()
+    n, width = args.served_jobs, int(args.served_window)
+    jobs = []
+    for i in range(n):
+        (b, s, ks, nl), (p0, _) = S.batch_job(1, i)
+        jobs.append((S.to_abcd(b, s, ks, nl), p0, p0 + width - 1))
+    total_width = n * width
+
+    def key(f):
+        return [(int(p), int(k), int(q)) for p, k, q in f]
+
+    # warm-up: the shared sieving primes up to sqrt of the largest p, module load
+    top = max(jobs, key=lambda j: j[2])
+    with rsieve.Job(top[0]) as j:
+        j.sieve(top[2] - 10**6, top[2])
+    t0 = time.perf_counter()
+    plain = []
+    for abcd, p0, p1 in jobs:
+        with rsieve.Job(abcd) as j:
+            f, _ = j.sieve(p0, p1)
+        plain.append(key(f))
+    t_plain = time.perf_counter() - t0
+
+    def run_server(arrivals):
+        """Submit job i at arrivals[i] seconds (None: all at once); return (reports, span)."""
+        reps = [None] * n
+        same = [True]
+        with rsieve.Server(slots=args.slots) as srv:
+            tickets = []
+            lock = threading.Lock()
+            ready = threading.Semaphore(0)
+
+            def collect():
+                for i in range(n):
+                    ready.acquire()
+                    with lock:
+                        t = tickets[i]
+                    f, rep = srv.wait(t)
+                    reps[i] = rep
+                    if key(f) != plain[i]:
+                        same[0] = False
+
+            th = threading.Thread(target=collect)
+            th.start()
+            start = time.perf_counter()
+            for i, (abcd, p0, p1) in enumerate(jobs):
+                if arrivals is not None:
+                    delay = start + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                t = srv.submit(abcd, p0, p1)
+                with lock:
+                    tickets.append(t)
+                ready.release()
+            th.join()
+            span = time.perf_counter() - start
+        return reps, span, same[0]
+
+    reps, t_batch, ok_batch = run_server(None)
+    capacity = n / t_batch  # jobs per second
+    served = []
+    ok_served = True
+    for load in args.served_loads:
+        rng = np.random.default_rng(1000 + int(load * 100))
+        arrivals = np.cumsum(rng.exponential(1.0 / (load * capacity), size=n)).tolist()
+        reps_l, span, ok = run_server(arrivals)
+        ok_served &= ok
+        lat = sorted(r["latency_ms"] for r in reps_l)
+        served.append({"load": load, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                       "p_per_s": total_width / span, "span_s": span})
+    at1 = min(served, key=lambda x: abs(x["load"] - 1.0)) if served else None
+    out = {
+        "metric": "served p99 job latency (mixed jobs, Poisson arrivals at 1.0x batched capacity)",
+        "value": at1["p99_ms"] if at1 else None, "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+        "dtype": "u64", "data": "synthetic (seeded)",
+        "config": {"workload": f"{n} jobs of rsieve.synth.batch_job(1, i), p-window {width} wide each",
+                   "slots": args.slots, "mem_budget_gib": 64, "queue_cap": 1024},
+        "plain": {"p_per_s": total_width / t_plain, "wall_s": t_plain},
+        "batched": {"p_per_s": total_width / t_batch, "wall_s": t_batch, "vs_plain": t_plain / t_batch,
+                    "jobs_per_s": capacity},
+        "served": served,
+        "results_match_plain": bool(ok_batch and ok_served),
+    }
+    print(json.dumps(out))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -242,7 +350,17 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--Q", type=int, default=0, help="force the subsequence modulus (default: planner)")
     ap.add_argument("--hash-m", type=int, default=0, help="cap baby steps at 2<<M (default: planner)")
+    ap.add_argument("--served", action="store_true",
+                    help="instead: plain vs batched vs served runs of the mixed-job stream (one JSON line)")
+    ap.add_argument("--served-jobs", type=int, default=64)
+    ap.add_argument("--served-window", type=float, default=1e8,
+                    help="p-window width of each job (the batch shape's 1e9 makes a run of 64 jobs take ~10 min)")
+    ap.add_argument("--served-loads", type=float, nargs="*", default=[0.5, 1.0, 1.5])
+    ap.add_argument("--slots", type=int, default=4, help="jobs running at once in the served form")
     args = ap.parse_args()
+    if args.served:
+        run_served(args)
+        return
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)

@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -318,8 +319,27 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
 // ---------------------------------------------------------------------------
 // The job.
 
+// Sieving primes of one device: odd primes <= limit with floor(2^64/q), shared
+// by every job on that device (a job keeps the set it started with alive).
+struct DevPrimes {
+  int device = 0;
+  uint64_t limit = 0;
+  uint32_t n = 0, nsmall = 0;
+  uint32_t *d_sp = nullptr;
+  uint64_t *d_rcp = nullptr;
+  ~DevPrimes() {
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return;
+    cudaSetDevice(device);
+    if (d_sp) cudaFree(d_sp);
+    if (d_rcp) cudaFree(d_rcp);
+    cudaSetDevice(cur);
+  }
+};
+
 struct rs_job {
   std::mutex mu;
+  std::shared_ptr<DevPrimes> primes;  // sieving primes in use (d_sp, d_sp_rcp below point into it)
   rs_options opt;
   Seqs seqs;
   Plan plan;
@@ -349,6 +369,33 @@ struct rs_job {
 };
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Pinned host blocks for the per-chunk prime counts, kept for reuse by later
+// jobs: freeing pinned memory synchronises the whole device, which would stall
+// the other jobs of a server.  Device buffers are stream-ordered
+// (cudaMallocAsync / cudaFreeAsync on the job's stream) for the same reason.
+static std::mutex g_pin_mu;
+static std::vector<std::pair<void *, size_t>> g_pin_free;
+
+static void *pinned_get(size_t bytes) {
+  bytes = align_up(bytes, 4096);
+  {
+    std::lock_guard<std::mutex> lock(g_pin_mu);
+    for (size_t i = 0; i < g_pin_free.size(); i++)
+      if (g_pin_free[i].second == bytes) {
+        void *p = g_pin_free[i].first;
+        g_pin_free.erase(g_pin_free.begin() + i);
+        return p;
+      }
+  }
+  void *p = nullptr;
+  return cudaMallocHost(&p, bytes) == cudaSuccess ? p : nullptr;
+}
+
+static void pinned_put(void *p, size_t bytes) {
+  std::lock_guard<std::mutex> lock(g_pin_mu);
+  g_pin_free.push_back({p, align_up(bytes, 4096)});
+}
 
 static int upload_job(rs_job *j) {
   const Plan &pl = j->plan;
@@ -419,7 +466,7 @@ static int upload_job(rs_job *j) {
   memcpy(host.data() + o_kj, kjac.data(), nk * 4);
   memcpy(host.data() + o_tk, tab_k.data(), tab_k.size() * 4);
   memcpy(host.data() + o_to, tab_off.data(), tab_off.size() * 4);
-  CUDA_TRY(cudaMalloc(&j->d_job, off));
+  CUDA_TRY(cudaMallocAsync(&j->d_job, off, j->st));
   CUDA_TRY(cudaMemcpyAsync(j->d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
   uint8_t *b = (uint8_t *)j->d_job;
   CUDA_TRY(launch_jacobi_tables((const uint32_t *)(b + o_tk), (const uint32_t *)(b + o_to),
@@ -487,43 +534,58 @@ static int upload_job(rs_job *j) {
 }
 
 // Odd primes <= limit by a simple sieve (the reference builds its small-prime
-// table on the host too, kernel_v0.24.6.cu:1271-1303).
+// table on the host too, kernel_v0.24.6.cu:1271-1303).  One set per device is
+// kept for the life of the process and grown when a job needs a larger limit,
+// so jobs after the first (a server's stream of jobs, a CLI resuming) reuse it.
+static std::mutex g_primes_mu;
+static std::shared_ptr<DevPrimes> g_primes[64];
+
 static int ensure_sieving_primes(rs_job *j, uint64_t hi, uint64_t *h2d = nullptr) {
   uint64_t r = (uint64_t)std::sqrt((long double)hi);
   while (r * r > hi) r--;
   while ((r + 1) * (r + 1) <= hi) r++;
-  if (j->d_sp && r <= j->sp_limit) return RS_OK;
-  uint64_t limit = std::max<uint64_t>(r, std::min<uint64_t>(2 * r, 1ull << 22));
-  std::vector<uint8_t> comp(limit / 2 + 1, 0);
-  std::vector<uint32_t> ps;
-  std::vector<uint64_t> rc;
-  for (uint64_t i = 3; i <= limit; i += 2) {
-    if (comp[i / 2]) continue;
-    ps.push_back((uint32_t)i);
-    rc.push_back((~0ull) / i);
-    for (uint64_t q = i * i; q <= limit; q += 2 * i) comp[q / 2] = 1;
+  if (j->primes && r <= j->primes->limit) return RS_OK;
+  if (j->device < 0 || j->device >= 64) return fail(RS_ERR_INVALID, "device ordinal %d", j->device);
+  std::lock_guard<std::mutex> lock(g_primes_mu);
+  std::shared_ptr<DevPrimes> &slot = g_primes[j->device];
+  if (!slot || slot->limit < r) {
+    const uint64_t limit = std::max<uint64_t>(r, std::min<uint64_t>(2 * r, 1ull << 22));
+    std::vector<uint8_t> comp(limit / 2 + 1, 0);
+    std::vector<uint32_t> ps;
+    std::vector<uint64_t> rc;
+    for (uint64_t i = 3; i <= limit; i += 2) {
+      if (comp[i / 2]) continue;
+      ps.push_back((uint32_t)i);
+      rc.push_back((~0ull) / i);
+      for (uint64_t q = i * i; q <= limit; q += 2 * i) comp[q / 2] = 1;
+    }
+    auto dp = std::make_shared<DevPrimes>();
+    dp->device = j->device;
+    dp->limit = limit;
+    CUDA_TRY(cudaMalloc(&dp->d_sp, std::max<size_t>(1, ps.size()) * 4));
+    CUDA_TRY(cudaMalloc(&dp->d_rcp, std::max<size_t>(1, rc.size()) * 8));
+    CUDA_TRY(cudaMemcpyAsync(dp->d_sp, ps.data(), ps.size() * 4, cudaMemcpyHostToDevice, j->st));
+    CUDA_TRY(cudaMemcpyAsync(dp->d_rcp, rc.data(), rc.size() * 8, cudaMemcpyHostToDevice, j->st));
+    CUDA_TRY(cudaStreamSynchronize(j->st));
+    dp->n = (uint32_t)ps.size();
+    dp->nsmall = (uint32_t)(std::lower_bound(ps.begin(), ps.end(), (uint32_t)(2 * kSieveOdds)) - ps.begin());
+    if (h2d) *h2d += ps.size() * 12;
+    slot = dp;
   }
-  if (j->d_sp) cudaFree(j->d_sp);
-  if (j->d_sp_rcp) cudaFree(j->d_sp_rcp);
-  j->d_sp = nullptr;
-  j->d_sp_rcp = nullptr;
-  CUDA_TRY(cudaMalloc(&j->d_sp, std::max<size_t>(1, ps.size()) * 4));
-  CUDA_TRY(cudaMalloc(&j->d_sp_rcp, std::max<size_t>(1, rc.size()) * 8));
-  CUDA_TRY(cudaMemcpyAsync(j->d_sp, ps.data(), ps.size() * 4, cudaMemcpyHostToDevice, j->st));
-  CUDA_TRY(cudaMemcpyAsync(j->d_sp_rcp, rc.data(), rc.size() * 8, cudaMemcpyHostToDevice, j->st));
-  CUDA_TRY(cudaStreamSynchronize(j->st));
-  j->nsp = (uint32_t)ps.size();
-  j->nsp_small = (uint32_t)(std::lower_bound(ps.begin(), ps.end(), (uint32_t)(2 * kSieveOdds)) - ps.begin());
-  j->sp_limit = limit;
-  if (h2d) *h2d += ps.size() * 12;
+  j->primes = slot;
+  j->d_sp = slot->d_sp;
+  j->d_sp_rcp = slot->d_rcp;
+  j->nsp = slot->n;
+  j->nsp_small = slot->nsmall;
+  j->sp_limit = slot->limit;
   return RS_OK;
 }
 
 static int ensure_gbits(rs_job *j, uint64_t words) {
   if (j->d_gbits && j->gbits_words >= words) return RS_OK;
-  if (j->d_gbits) cudaFree(j->d_gbits);
+  if (j->d_gbits) cudaFreeAsync(j->d_gbits, j->st);
   j->d_gbits = nullptr;
-  CUDA_TRY(cudaMalloc(&j->d_gbits, words * 4));
+  CUDA_TRY(cudaMallocAsync(&j->d_gbits, words * 4, j->st));
   j->gbits_words = words;
   return RS_OK;
 }
@@ -532,7 +594,7 @@ static size_t chunk_bytes_per_prime(const rs_job *j) { return 8 + 4 + 8 * (size_
 
 static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   if (j->d_chunk && j->chunk_cap >= cap) return RS_OK;
-  if (j->d_chunk) cudaFree(j->d_chunk);
+  if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
   j->d_chunk = nullptr;
   size_t off = 0;
   auto sec = [&](size_t bytes) {
@@ -542,7 +604,7 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   };
   const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * 8 * j->dev.rec_elems);
   const size_t o_rd = sec((size_t)cap * 4), o_rc = sec(16);
-  CUDA_TRY(cudaMalloc(&j->d_chunk, off));
+  CUDA_TRY(cudaMallocAsync(&j->d_chunk, off, j->st));
   uint8_t *b = (uint8_t *)j->d_chunk;
   j->cb.primes = (uint64_t *)(b + o_pr);
   j->cb.count = (uint32_t *)(b + o_ct);
@@ -556,7 +618,7 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
 
 static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
   if (j->d_hits && j->hb.cap >= cap) return RS_OK;
-  if (j->d_hits) cudaFree(j->d_hits);
+  if (j->d_hits) cudaFreeAsync(j->d_hits, j->st);
   j->d_hits = nullptr;
   size_t off = 0;
   auto sec = [&](size_t bytes) {
@@ -566,7 +628,7 @@ static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
   };
   const size_t o_raw = sec((size_t)cap * sizeof(Hit)), o_rc = sec(16);
   const size_t o_fac = sec((size_t)cap * sizeof(Hit)), o_fc = sec(16);
-  CUDA_TRY(cudaMalloc(&j->d_hits, off));
+  CUDA_TRY(cudaMallocAsync(&j->d_hits, off, j->st));
   uint8_t *b = (uint8_t *)j->d_hits;
   j->hb.raw = (Hit *)(b + o_raw);
   j->hb.raw_count = (uint32_t *)(b + o_rc);
@@ -579,13 +641,14 @@ static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
 static void free_job(rs_job *j) {
   if (!j) return;
   if (j->st) cudaStreamSynchronize(j->st);
-  if (j->d_job) cudaFree(j->d_job);
-  if (j->d_sp) cudaFree(j->d_sp);
-  if (j->d_sp_rcp) cudaFree(j->d_sp_rcp);
-  if (j->d_chunk) cudaFree(j->d_chunk);
-  if (j->d_hits) cudaFree(j->d_hits);
-  if (j->d_gbits) cudaFree(j->d_gbits);
-  if (j->h_counts) cudaFreeHost(j->h_counts);
+  if (j->st) {
+    if (j->d_job) cudaFreeAsync(j->d_job, j->st);
+    if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
+    if (j->d_hits) cudaFreeAsync(j->d_hits, j->st);
+    if (j->d_gbits) cudaFreeAsync(j->d_gbits, j->st);
+    cudaStreamSynchronize(j->st);
+  }
+  if (j->h_counts) pinned_put(j->h_counts, j->h_counts_cap * 4);
   if (j->st) cudaStreamDestroy(j->st);
   delete j;
 }
@@ -634,7 +697,8 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out) {
     cap = (uint64_t)128 << (bs - 1);
     cap *= (uint64_t)128 << (ts - 1);
   } else {
-    cap = (2ull << 30) / chunk_bytes_per_prime(j);
+    const uint64_t budget = opt.mem_limit ? opt.mem_limit : (2ull << 30);
+    cap = budget / chunk_bytes_per_prime(j);
   }
   cap = std::max<uint64_t>(cap, 4096);
   cap = std::min<uint64_t>(cap, 1u << 23);
@@ -792,13 +856,13 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
   uint64_t total_primes = 0;
   for (int attempt = 0; attempt < 8 && !todo.empty(); attempt++) {
     if (j->h_counts_cap < todo.size() + 2) {
-      if (j->h_counts) cudaFreeHost(j->h_counts);
+      if (j->h_counts) pinned_put(j->h_counts, j->h_counts_cap * 4);
       j->h_counts = nullptr;
       j->h_counts_cap = todo.size() + 2;
-      cudaError_t e = cudaMallocHost(&j->h_counts, j->h_counts_cap * 4);
-      if (e != cudaSuccess) {
+      j->h_counts = (uint32_t *)pinned_get(j->h_counts_cap * 4);
+      if (!j->h_counts) {
         cleanup_events();
-        return fail(RS_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e));
+        return fail(RS_ERR_NOMEM, "cudaMallocHost failed");
       }
     }
     // (re)create timing events: 6 per chunk
@@ -1025,10 +1089,11 @@ extern "C" int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap
     ~Guard() {
       if (d_out) cudaFree(d_out);
       if (d_cnt) cudaFree(d_cnt);
-      if (t.d_sp) cudaFree(t.d_sp);
-      if (t.d_sp_rcp) cudaFree(t.d_sp_rcp);
-      if (t.d_gbits) cudaFree(t.d_gbits);
-      if (t.st) cudaStreamDestroy(t.st);
+      if (t.d_gbits && t.st) cudaFreeAsync(t.d_gbits, t.st);
+      if (t.st) {
+        cudaStreamSynchronize(t.st);
+        cudaStreamDestroy(t.st);
+      }
       t.d_gbits = nullptr;
       t.d_sp = nullptr;
       t.d_sp_rcp = nullptr;

@@ -926,7 +926,14 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 int bsgs_exact_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (4 << job.exact_log2); }
 
 static cudaError_t configure_one(const void *fn, int smem, int device, int *grid_out) {
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  // The limit is a property of the kernel shared by every job in the process,
+  // so it is set to the device maximum (the same value from every thread)
+  // rather than to this job's size, which a concurrent job could lower.
+  int max_smem = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e != cudaSuccess) return e;
+  if (smem > max_smem) return cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;

@@ -21,6 +21,8 @@ RS_ERR_RANGE = 4
 RS_ERR_NODEVICE = 5
 RS_ERR_CAPACITY = 6
 RS_ERR_INTERNAL = 7
+RS_ERR_BUSY = 8
+RS_ERR_TIMEOUT = 9
 
 FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u4"), ("n", "<u4")])
 
@@ -29,7 +31,8 @@ EXPORTS = (
     "rs_options_default", "rs_job_create_abcd", "rs_job_create", "rs_job_info_get",
     "rs_plan_abcd", "rs_job_destroy", "rs_sieve_range", "rs_write_factors", "rs_gpu_primes",
     "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
-    "rs_abcd_remove",
+    "rs_abcd_remove", "rs_server_options_default", "rs_server_create", "rs_server_submit",
+    "rs_server_wait", "rs_server_destroy",
 )
 
 
@@ -49,6 +52,8 @@ class Options(ctypes.Structure):
         ("datless", ctypes.c_int32),
         ("host_verify", ctypes.c_int32),
         ("device", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("mem_limit", ctypes.c_uint64),
     ]
 
 
@@ -96,6 +101,33 @@ class Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [
+        ("device", ctypes.c_int32),
+        ("slots", ctypes.c_uint32),
+        ("queue_cap", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("mem_budget", ctypes.c_uint64),
+    ]
+
+
+class JobReport(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("reserved", ctypes.c_uint32),
+        ("primes", ctypes.c_uint64),
+        ("factors", ctypes.c_uint64),
+        ("p_covered", ctypes.c_uint64),
+        ("queue_ms", ctypes.c_double),
+        ("run_ms", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+        ("gpu_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 _lib = None
 
 
@@ -122,6 +154,13 @@ def lib():
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
         L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
         L.rs_abcd_remove.argtypes = [ctypes.c_char_p, sz, vp, sz, u64, vp, sz, ctypes.POINTER(sz)]
+        L.rs_server_options_default.argtypes = [ctypes.POINTER(ServerOptions)]
+        L.rs_server_options_default.restype = None
+        L.rs_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
+        L.rs_server_submit.argtypes = [vp, ctypes.c_char_p, sz, ctypes.POINTER(Options), u64, u64,
+                                       ctypes.POINTER(u64)]
+        L.rs_server_wait.argtypes = [vp, u64, i32, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(JobReport)]
+        L.rs_server_destroy.argtypes = [vp]
         L.rs_last_error.restype = ctypes.c_char_p
         L.rs_version.restype = ctypes.c_char_p
         _lib = L
@@ -201,6 +240,63 @@ class Job:
     def close(self) -> None:
         if self._h:
             lib().rs_job_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A job server on one GPU (rs_server_*): jobs run concurrently in `slots`."""
+
+    def __init__(self, device: int = 0, slots: int = 0, queue_cap: int = 0, mem_budget: int = 0):
+        self._h = ctypes.c_void_p(None)
+        o = ServerOptions()
+        lib().rs_server_options_default(ctypes.byref(o))
+        o.device = device
+        if slots:
+            o.slots = slots
+        if queue_cap:
+            o.queue_cap = queue_cap
+        if mem_budget:
+            o.mem_budget = mem_budget
+        _check(lib().rs_server_create(ctypes.byref(o), ctypes.byref(self._h)))
+
+    def submit(self, abcd: str | bytes, p0: int, p1: int, **opts) -> int:
+        if isinstance(abcd, str):
+            abcd = abcd.encode()
+        t = ctypes.c_uint64(0)
+        _check(lib().rs_server_submit(self._h, abcd, len(abcd), ctypes.byref(make_options(**opts)), p0, p1,
+                                      ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(factors, report dict) of a finished job; raises RsieveError(RS_ERR_TIMEOUT) if still running."""
+        cap = 1 << 12
+        while True:
+            out = np.zeros(cap, dtype=FACTOR_DTYPE)
+            cnt = ctypes.c_size_t(0)
+            rep = JobReport()
+            rc = lib().rs_server_wait(self._h, ticket, timeout_ms, out.ctypes.data, cap, ctypes.byref(cnt),
+                                      ctypes.byref(rep))
+            if rc == RS_ERR_CAPACITY:
+                cap = cnt.value
+                continue
+            _check(rc)
+            return out[: cnt.value], rep.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            lib().rs_server_destroy(self._h)
             self._h = ctypes.c_void_p(None)
 
     def __enter__(self):

@@ -40,6 +40,8 @@ extern "C" {
 #define RS_ERR_NODEVICE 5  /* no CUDA device (the library has no CPU path) */
 #define RS_ERR_CAPACITY 6  /* output buffer too small; *count holds the size needed */
 #define RS_ERR_INTERNAL 7  /* a reported factor failed host re-verification */
+#define RS_ERR_BUSY 8      /* server queue full: retry later */
+#define RS_ERR_TIMEOUT 9   /* rs_server_wait: the job has not finished yet */
 
 typedef struct rs_job rs_job;
 
@@ -64,6 +66,9 @@ typedef struct {
   int32_t host_verify;  /* re-verify every factor on the host with 128-bit
                            arithmetic (kernel_v0.24.6.cu:1649-1671); default 1 */
   int32_t device;       /* CUDA device ordinal (the reference hard-codes 0) */
+  int32_t reserved;     /* 0 */
+  uint64_t mem_limit;   /* device bytes for the job's per-launch buffers, which set the
+                           primes per launch when -b/-t are not given; 0 = 2 GiB */
 } rs_options;
 
 /* The plan a job runs with. */
@@ -183,6 +188,58 @@ int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, 
 
 const char *rs_last_error(void);
 const char *rs_version(void);
+
+/* ------------------------------------------------------------------------
+ * Serving (no counterpart in the reference, which runs one job per process).
+ * A server owns a device and runs submitted jobs concurrently: each of
+ * `slots` worker threads admits the oldest waiting job when it is free, creates
+ * it, sieves its range on its own stream and releases it, so jobs that arrive
+ * while others run overlap on the GPU.  Device memory is partitioned: every
+ * running job's per-launch buffers are limited to mem_budget / slots.  Results
+ * are identical to running each job alone through rs_job_create_abcd +
+ * rs_sieve_range (the same kernels on the same inputs).
+ * ------------------------------------------------------------------------ */
+typedef struct rs_server rs_server;
+
+typedef struct {
+  int32_t device;       /* CUDA device ordinal */
+  uint32_t slots;       /* jobs running at once; 0 = 4 */
+  uint32_t queue_cap;   /* jobs waiting for a slot before submit returns RS_ERR_BUSY; 0 = 1024 */
+  uint32_t reserved;    /* 0 */
+  uint64_t mem_budget;  /* device bytes shared by the running jobs; 0 = 64 GiB */
+} rs_server_options;
+
+/* Timing and counters of one served job (host clock unless noted). */
+typedef struct {
+  int32_t status;       /* the job's rs_* status */
+  uint32_t reserved;
+  uint64_t primes;      /* primes sieved */
+  uint64_t factors;     /* factors found */
+  uint64_t p_covered;   /* width of the p-interval covered */
+  double queue_ms;      /* submit -> admitted to a slot */
+  double run_ms;        /* admitted -> finished (job creation, sieve, release) */
+  double latency_ms;    /* submit -> finished */
+  double gpu_ms;        /* CUDA-event time of the job's kernels */
+} rs_job_report;
+
+void rs_server_options_default(rs_server_options *opt);
+int rs_server_create(const rs_server_options *opt, rs_server **server);
+/* Queue a job: the ABCD text (copied), its options (mem_limit is set by the
+ * server) and the range [p0, p1].  *ticket identifies it to rs_server_wait.
+ * RS_ERR_BUSY when queue_cap jobs are already waiting. */
+int rs_server_submit(rs_server *server, const char *abcd, size_t len, const rs_options *opt, uint64_t p0,
+                     uint64_t p1, uint64_t *ticket);
+/* Wait up to timeout_ms (< 0: no limit) for a job.  RS_ERR_TIMEOUT if it has
+ * not finished.  When it has: its factors (sorted by (p, k, n)) go to out and
+ * *count, the report to *report (may be NULL), the ticket is released and the
+ * job's own status is returned (its message via rs_last_error).  If more than
+ * cap factors were found, RS_ERR_CAPACITY with *count = the number found; the
+ * ticket stays valid for another call. */
+int rs_server_wait(rs_server *server, uint64_t ticket, int32_t timeout_ms, rs_factor *out, size_t cap,
+                   size_t *count, rs_job_report *report);
+/* Let running jobs finish, drop waiting ones, stop the workers, free.  No
+ * rs_server_wait may be in progress or follow (the tickets die with it). */
+int rs_server_destroy(rs_server *server);
 
 #ifdef __cplusplus
 }

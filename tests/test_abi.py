@@ -89,6 +89,9 @@ def test_no_cpu_fallback(rs):
     assert e.value.code == rs.RS_ERR_NODEVICE
     with pytest.raises(rs.RsieveError):
         rs.gpu_primes(3, 1000)
+    with pytest.raises(rs.RsieveError) as e:
+        rs.Server()
+    assert e.value.code == rs.RS_ERR_NODEVICE
 
 
 def test_cli_help(rs):
