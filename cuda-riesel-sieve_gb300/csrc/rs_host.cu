@@ -175,12 +175,15 @@ static void normalise(Seqs &s) {
 struct Plan {
   uint32_t Q = 0, nrows = 0, X = 0, x_lo = 0, x_hi = 0, m = 0, T = 0;
   uint32_t tlanes = 0, rows_per_it = 0, steps_per_lane = 0, table_log2 = 0, jbits = 0, bucket_log2 = 0;
+  bool cta = false;  // one CTA of kCtaWarps warps per prime (bsgs_cta_kernel)
   uint32_t nmin = 0, nmax = 0, ncand = 0, words_per_row = 0;
   int64_t e0 = 0;
   double cost = 0, work_per_prime = 0;
   std::vector<uint32_t> row_r, row_kidx, k_row0;
   std::vector<uint32_t> bitmap;
 };
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 static uint32_t ilog2_ceil(uint64_t v) {
   uint32_t b = 0;
@@ -228,28 +231,18 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
     if (opt.hash_m > 14) return fail(RS_ERR_INVALID, "-m %d too large (at most 14)", opt.hash_m);
     mcap = std::min<uint64_t>(mcap, (uint64_t)2 << opt.hash_m);
   }
+  // Shared memory of an SM, and the warps per SM the warp-per-prime kernel
+  // reaches with small tables (registers allow 5 CTAs of 4 warps).
+  constexpr double kSmemPerSm = 233472.0, kFullWarps = 20.0;
+  // A giant step (Shoup product + probe) costs about 1.4 baby steps (a short or
+  // Shoup product + insert), measured on the benchmark job.
+  constexpr double kGiantWeight = 1.4;
   double best = 1e300;
   for (uint32_t Q : Qs) {
     const uint32_t X = nmax / Q - nmin / Q + 1;
     const int rows = count_rows(s, Q, datless);
     const double ER = rows * ((Q & 1) ? 0.75 : 0.5);
-    for (uint32_t tl = 0; tl <= 20; tl++) {
-      const uint64_t T = (uint64_t)1 << tl;
-      uint64_t m = (X + T - 1) / T;
-      // whole baby chains (64 chains of equal length) when that stays within the cap
-      if (m > 64 && ((m + 63) & ~63ull) <= mcap) m = (m + 63) & ~63ull;
-      if (m > mcap) continue;
-      if (m * T < X) continue;
-      const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));  // exact-path table
-      if (slog > kMaxTableLog2) continue;
-      const uint32_t tlanes = (uint32_t)std::min<uint64_t>(T, 32);
-      const uint32_t rpi = 32 / tlanes;
-      const uint32_t spl = (uint32_t)std::max<uint64_t>(1, T / 32);
-      // Per-lane units of one baby or giant step (a Shoup product plus a table
-      // operation, about equal on GB300), the table clear, and the per-prime
-      // setup kernel, whose measured cost grows with the number of rows.
-      double cost = std::ceil((double)m / 32.0) + std::ceil(ER / rpi) * spl +
-                    (double)(1u << slog) / 1024.0 + 3.7 + 0.062 * rows;
+    auto consider = [&](bool cta, uint64_t T, uint64_t m, uint32_t blog, uint32_t slog, double cost) {
       if (cost < best) {
         best = cost;
         pl.Q = Q;
@@ -257,12 +250,62 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
         pl.X = X;
         pl.m = (uint32_t)m;
         pl.T = (uint32_t)T;
-        pl.tlanes = tlanes;
-        pl.rows_per_it = rpi;
-        pl.steps_per_lane = spl;
+        pl.tlanes = (uint32_t)std::min<uint64_t>(T, 32);
+        pl.rows_per_it = 32 / pl.tlanes;
+        pl.steps_per_lane = (uint32_t)std::max<uint64_t>(1, T / 32);
         pl.table_log2 = slog;
+        pl.bucket_log2 = blog;
+        pl.cta = cta;
         pl.cost = cost;
         pl.work_per_prime = 2.0 * std::sqrt(ER * (double)X);
+      }
+    };
+    for (uint32_t tl = 0; tl <= 20; tl++) {
+      const uint64_t T = (uint64_t)1 << tl;
+      const uint64_t m0 = (X + T - 1) / T;
+      const uint32_t tlanes = (uint32_t)std::min<uint64_t>(T, 32);
+      const uint32_t rpi = 32 / tlanes;
+      const uint32_t spl = (uint32_t)std::max<uint64_t>(1, T / 32);
+      // Costs are in warp-steps per prime: one baby or giant step of 32 lanes
+      // (a product plus a table operation), the table clear, the per-prime
+      // setup kernel (grows with the rows), the expected tag-match
+      // resolution (one pass over the baby steps), and a penalty for fewer
+      // resident warps when the tables are large.
+      {  // warp per prime: whole chains of 64 when that stays within the cap
+        uint64_t m = m0;
+        if (m > 64 && ((m + 63) & ~63ull) <= mcap) m = (m + 63) & ~63ull;
+        const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));  // exact-path table
+        if (m <= mcap && m * T >= X && slog <= kMaxTableLog2) {
+          const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((2 * m + kBucket - 1) / kBucket));
+          const double nb = (double)(1u << blog);
+          // the kernel's shared memory per warp and per CTA (128-byte granules, 1 KB reserved)
+          const uint64_t stage = kElV + ((rows + 1) & ~1u);
+          const uint64_t wsm = align_up((20u << blog) + 16 * (stage * 8 <= 2048 ? stage : kElV) + 16 * kMatchCap + 16, 16);
+          const double cta_bytes = (double)align_up(4 * wsm, 128) + 1024.0;
+          const double warps = std::min(kFullWarps, 4.0 * std::floor(kSmemPerSm / cta_bytes));
+          if (warps >= 4) {
+            const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+            const double cost = (std::ceil((double)m / 32.0) + kGiantWeight * std::ceil(ER / rpi) * spl +
+                                 nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
+                                std::sqrt(kFullWarps / warps);
+            consider(false, T, m, blog, slog, cost);
+          }
+        }
+      }
+      if (T >= 32) {  // a CTA per prime: 64 * kCtaWarps chains share a table of up to ~160 KB
+        const uint64_t chains = 64 * kCtaWarps;
+        const uint64_t m = (m0 + chains - 1) / chains * chains;
+        const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));
+        const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((m + 1) / 2));  // <= 2 entries per bucket
+        const double nb = (double)(1u << blog);
+        const double smem = 20.0 * nb + 8.0 * (rows + 2) + 16.0 * (kCtaMatchCap + 1);
+        if (m <= mcap && m * T >= X && slog <= 15 && smem <= 232448.0) {
+          const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+          const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
+                               nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
+                              std::sqrt(kFullWarps / kCtaWarps);
+          consider(true, T, m, blog, slog, cost);
+        }
       }
     }
   }
@@ -275,8 +318,6 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
   pl.e0 = (int64_t)pl.x_lo - 1;
   pl.jbits = 1;
   while (((uint64_t)1 << pl.jbits) < (uint64_t)pl.m + 1) pl.jbits++;
-  // fast-path buckets: 7 16-bit tags each, at most about 2/7 full on average
-  pl.bucket_log2 = std::max<uint32_t>(4, ilog2_ceil((2 * (uint64_t)pl.m + kBucket - 1) / kBucket));
   pl.words_per_row = (pl.X + 31) / 32;
   // rows: k in input order, r ascending
   const uint32_t Q = pl.Q;
@@ -368,7 +409,6 @@ struct rs_job {
   uint32_t chunk_cap = 0;
 };
 
-static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Pinned host blocks for the per-chunk prime counts, kept for reuse by later
 // jobs: freeing pinned memory synchronises the whole device, which would stall
@@ -477,7 +517,8 @@ static int upload_job(rs_job *j) {
   d.sign = s.sign;
   d.Q = pl.Q;
   d.m = pl.m;
-  d.chain_len = (pl.m + 63) / 64;
+  d.cta_warps = pl.cta ? kCtaWarps : 1;
+  d.chain_len = (pl.m + 64 * d.cta_warps - 1) / (64 * d.cta_warps);
   {
     uint64_t bq = 1;
     for (uint32_t q = 0; q < pl.Q && bq; q++) bq = (bq * s.base < (1ull << 32)) ? bq * s.base : 0;
@@ -500,7 +541,8 @@ static int upload_job(rs_job *j) {
   d.words_per_row = pl.words_per_row;
   d.datless = j->opt.datless ? 1u : 0u;
   d.max_act = std::max<uint32_t>(1, pl.nrows);
-  d.el_row = kElV + ((d.max_act + 1) & ~1u);  // even: row ids are written 16 bytes at a time
+  d.el_v = d.cta_warps > 1 ? kElWoff + 2 * d.cta_warps : kElV;
+  d.el_row = d.el_v + ((d.max_act + 1) & ~1u);  // even: row ids are written 16 bytes at a time
   d.el_tab = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
   d.rec_elems = d.el_tab + 64;
   if (d.el_row * 8 <= 2048) {
@@ -508,9 +550,12 @@ static int upload_job(rs_job *j) {
     d.stage_elems = d.el_row;
   } else {
     d.stage_full = 0;
-    d.stage_elems = kElV;
+    d.stage_elems = d.el_v;
   }
-  d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
+  if (d.cta_warps > 1)  // bytes per CTA: table, counts, V, match list
+    d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 8 * ((d.max_act + 1) & ~1u) + kCtaMatchCap * 16 + 16, 16);
+  else  // bytes per warp: table, counts, two record stages, match list
+    d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.k_val = (const uint32_t *)(b + o_kv);

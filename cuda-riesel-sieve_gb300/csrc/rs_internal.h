@@ -26,19 +26,25 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // first el_row elements) into shared memory with 16-byte cp.async copies and
 // loads each lane's own table entries straight into registers.
 //
-// Baby steps run in 64 chains of chain_len consecutive exponents: chain c
-// covers j = c*chain_len + t, each step a product by B = b^Q.  Lane l owns
-// chains l and l + 32.  Element map:
+// Baby steps run in 64*W chains of chain_len consecutive exponents, W the
+// warps that share one prime (1 in the warp-per-prime kernel, kCtaWarps in the
+// CTA-per-prime kernel): chain c covers j = c*chain_len + t, each step a
+// product by B = b^Q.  Thread t of the prime's group (t = 32*warp + lane) owns
+// chains t and t + 32W.  Element map:
 //   0 p, 1 pinv, 2 B, 3 G^32 (giant stride), 4 nact, 5 floor(2^64 / p),
 //   6,7 B in normal form and its Shoup constant (the chain step),
-//   8,9 B^(32*chain_len) likewise (chain l -> chain l+32), 10,11 G^32 likewise,
-//   12.. V[max_act] (giant-step start per active row), el_row.. row ids (u16,
-//   4 per element), el_tab.. B^(lane*chain_len) (32 elements, the chain starts),
-//   el_tab+32.. G^(lane % tlanes + 1) (32 elements).
+//   8,9 B^(32W*chain_len) likewise (chain t -> chain t+32W), 10,11 G^32 likewise,
+//   W > 1 only: 12.. B^(32w*chain_len) for w < W likewise (pairs; warp w's offset),
+//   el_v.. V[max_act] (giant-step start per active row), el_row.. row ids (u16,
+//   4 per element), el_tab.. B^(lane*chain_len) (32 elements, the chain starts
+//   of warp 0), el_tab+32.. G^(lane % tlanes + 1) (32 elements).
 // Residues are in Montgomery form unless marked normal.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kElRcp = 5;
 constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
-constexpr uint32_t kElV = 12;
+constexpr uint32_t kElWoff = 12;   // warp offsets (W > 1)
+constexpr uint32_t kElV = 12;      // V in the warp-per-prime layout (W == 1)
+constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
+constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
 // Job constants, passed by value to every kernel (lives in the constant bank).
 struct JobDev {
@@ -46,7 +52,9 @@ struct JobDev {
   int32_t sign;          // -1 Riesel, +1 Sierpinski
   uint32_t Q;
   uint32_t m;            // baby steps per prime
-  uint32_t chain_len;    // baby steps per chain, ceil(m / 64)
+  uint32_t chain_len;    // baby steps per chain, m / (64 * cta_warps)
+  uint32_t cta_warps;    // warps per prime: 1 (bsgs_kernel) or kCtaWarps (bsgs_cta_kernel)
+  uint32_t el_v;         // first element of V (kElV, or kElWoff + 2*cta_warps)
   uint32_t bq_small;     // b^Q as an integer when below 2^32, else 0
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row

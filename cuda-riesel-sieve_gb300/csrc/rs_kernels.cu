@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           for (; cur < r; cur++) V = shoup_mul(V, bmod, bq, p);
         }
         if (nact & 1) {
-          if (live) rec_st2(rec, kElV + nact - 1, vprev, V);
+          if (live) rec_st2(rec, J.el_v + nact - 1, vprev, V);
         } else {
           vprev = V;
         }
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
     }
   }
   if (!live) return;
-  if (nact & 1) rec[kElV + nact - 1] = vprev;
+  if (nact & 1) rec[J.el_v + nact - 1] = vprev;
   if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBm, B, Gs);
@@ -374,8 +374,20 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   rec_st2(rec, kElNact, pb ? 0 : nact, shoup_const(one, M.pinv));
   // the strides in normal form with their Shoup constants, once per prime
   rec_st2(rec, kElStw, from_mont(B, p, M.pinv), shoup_const(B, M.pinv));
-  rec_st2(rec, kElOfw, from_mont(Bs, p, M.pinv), shoup_const(Bs, M.pinv));
   rec_st2(rec, kElGw, from_mont(Gs, p, M.pinv), shoup_const(Gs, M.pinv));
+  // chain offsets: warp w of a prime's group starts its chains at B^(32w*c),
+  // and a thread's second chain is 32W chains after its first
+  uint64_t off = Bs;  // B^(32*c)
+  if (J.cta_warps > 1) {
+    uint64_t o = one;
+#pragma unroll 1
+    for (uint32_t w = 0; w < J.cta_warps; w++) {
+      rec_st2(rec, kElWoff + 2 * w, from_mont(o, p, M.pinv), shoup_const(o, M.pinv));
+      o = montmul(o, Bs, M);
+    }
+    off = o;  // B^(32W*c)
+  }
+  rec_st2(rec, kElOfw, from_mont(off, p, M.pinv), shoup_const(off, M.pinv));
 }
 
 // Quadratic-character tables: word w of the table of odd k' holds bit t =
@@ -453,8 +465,6 @@ __device__ __forceinline__ void stage_copy(uint64_t *dst, const JobDev &J, const
 __device__ __forceinline__ void stage_commit_empty() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-constexpr int kOvfCap = 2 * kMatchCap;  // 8-byte values in the match list's space
 
 struct __align__(16) Match {
   uint64_t y;     // giant-step value whose tag matched
@@ -552,14 +562,15 @@ struct WarpTable {
 struct MatchList {
   Match *list;
   uint32_t *count;
-  // Baby-phase use of the same space: up to kOvfCap values to insert late.
+  uint32_t cap;  // matches the list holds; the baby phase's overflow values use the same space (2*cap)
+  // Baby-phase use of the same space: up to 2*cap values to insert late.
   __device__ __forceinline__ void append(uint64_t *ovf, uint64_t v) const {
     const uint32_t idx = atomicAdd(count, 1u);
-    if (idx < (uint32_t)kOvfCap) ovf[idx] = v;
+    if (idx < 2 * cap) ovf[idx] = v;
   }
   __device__ __forceinline__ void push(uint64_t y, uint32_t slot, uint32_t s) const {
     const uint32_t idx = atomicAdd(count, 1u);
-    if (idx < (uint32_t)kMatchCap) {
+    if (idx < cap) {
       Match mt;
       mt.y = y;
       mt.slot = slot;
@@ -656,6 +667,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   MatchList ML;
   ML.list = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
+  ML.cap = kMatchCap;
   const uint32_t lane_t = lane & (TL - 1);
   const uint32_t lane_row = lane / TL;
   const uint32_t total = *cb.count;
@@ -728,7 +740,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       }
       __syncwarp();
       const uint32_t novf = *ML.count;
-      if (novf > (uint32_t)kOvfCap) {  // pathological table: leave the prime to the exact path
+      if (novf > 2 * ML.cap) {  // pathological table: leave the prime to the exact path
         if (lane == 0) {
           const uint32_t r = atomicAdd(cb.redo_count, 1u);
           if (r < cb.cap) cb.redo[r] = i;
@@ -844,40 +856,185 @@ static BsgsFn bsgs_fn(uint32_t tlanes) {
   }
 }
 
-int bsgs_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (int)job.warp_smem; }
+int bsgs_smem_bytes(const JobDev &job) {
+  return job.cta_warps > 1 ? (int)job.warp_smem : kWarpsPerBlock * (int)job.warp_smem;
+}
 
-// The exact path: a per-warp table of (tag << jbits) | j entries with linear
-// probing, for the primes whose tag matches overflowed the fast path's list.
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+// The CTA-per-prime kernel, for jobs whose best baby-step count needs a table
+// larger than a warp's share of shared memory (many k, wide n ranges).  All
+// kCtaWarps warps of a CTA work on one prime: thread t runs baby chains t and
+// t + 32W into one table that fills most of the SM's shared memory, and warp w
+// takes the giant steps of row slots w, w + W, ... (32 lanes per row, T/32
+// steps per lane).  Shared memory:
+//   [NB buckets x 16 B][NB counts x 4 B][V, max_act x 8 B][kCtaMatchCap matches][count, 16 B]
+// V is staged with cp.async during the baby steps.  Table operations, the
+// deferred overflow inserts and the exact tag-match resolution are those of
+// bsgs_kernel; hits are pushed where they are found (tag matches are rare).
+__global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
+  extern __shared__ uint4 smem4[];
+  constexpr uint32_t G = 32 * kCtaWarps;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t NB = 1u << J.table_log2;
+  uint8_t *base = reinterpret_cast<uint8_t *>(smem4);
+  WarpTable W;
+  W.tab4 = reinterpret_cast<uint4 *>(base);
+  W.tab16 = reinterpret_cast<uint16_t *>(base);
+  W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
+  W.bmask = NB - 1;
+  uint64_t *vst = reinterpret_cast<uint64_t *>(base + NB * 20);
+  const uint32_t vst_elems = (J.max_act + 1) & ~1u;
+  MatchList ML;
+  ML.list = reinterpret_cast<Match *>(vst + vst_elems);
+  ML.count = reinterpret_cast<uint32_t *>(ML.list + kCtaMatchCap);
+  ML.cap = kCtaMatchCap;
+  uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
+  const uint32_t total = *cb.count;
+  const uint32_t n = total < cb.cap ? total : cb.cap;
+  const uint32_t CL = J.chain_len, spl = J.steps_per_lane;
+  const uint32_t ja0 = tid * CL, jb0 = (tid + G) * CL;  // the thread's chains; m == 2*G*CL
+  const uint32_t vdst = (uint32_t)__cvta_generic_to_shared(vst);
+
+#pragma unroll 1
+  for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    const uint64_t *rec = cb.recs + (size_t)i * J.rec_elems;
+    const uint32_t nact = (uint32_t)rec[kElNact];
+    if (nact == 0) continue;
+    const uint64_t p = rec[kElP], pinv = rec[kElPinv];
+    __syncthreads();  // the previous prime is done with the table, V and the list
+    // V of the active rows into shared memory, 16 bytes per copy
+    const uint32_t vn = (nact + 1) & ~1u;
+#pragma unroll 1
+    for (uint32_t e = 2 * tid; e < vn; e += 2 * G)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(vdst + 8 * e), "l"(rec + J.el_v + e)
+                   : "memory");
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    const uint4 z4 = make_uint4(0, 0, 0, 0);
+#pragma unroll 4
+    for (uint32_t q = tid; q < NB + NB / 4; q += G) W.tab4[q] = z4;
+    if (tid == 0) *ML.count = 0;
+    __syncthreads();
+
+    // Baby steps: chain starts B^(lane*c) times the warp's offset B^(32w*c)
+    uint64_t Bl = rec[J.el_tab + lane];
+    if (warp) Bl = shoup_mul(Bl, rec[kElWoff + 2 * warp], rec[kElWoff + 2 * warp + 1], p);
+    const uint64_t Blb = shoup_mul(Bl, rec[kElOfw], rec[kElOfq], p);
+    if (cb.small_step)
+      baby_chains<true>(W, ML, ovf, Bl, Blb, CL, CL, CL, StepSmall{J.bq_small, (uint32_t)rec[kElRcp], p});
+    else
+      baby_chains<true>(W, ML, ovf, Bl, Blb, CL, CL, CL, StepShoup{rec[kElStw], rec[kElStq], p});
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    const uint32_t novf = *ML.count;
+    if (novf > 2 * ML.cap) {  // pathological table: leave the prime to the exact path
+      if (tid == 0) {
+        const uint32_t r = atomicAdd(cb.redo_count, 1u);
+        if (r < cb.cap) cb.redo[r] = i;
+      }
+      continue;
+    }
+    if (novf) {
+      const uint64_t v = tid < novf ? ovf[tid] : 0;
+      __syncthreads();
+      if (tid == 0) *ML.count = 0;
+      if (tid < novf) W.insert_after((uint32_t)v, (uint32_t)v & W.bmask);
+      __syncthreads();
+    }
+
+    // Giant steps: warp w takes row slots w, w + W, ... two at a time
+    const uint64_t Glm = rec[J.el_tab + 32 + lane];
+    const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
+    const uint64_t Gw = rec[kElGw], Gq = rec[kElGq];
+#pragma unroll 1
+    for (uint32_t sa = warp; sa < nact; sa += 2 * kCtaWarps) {
+      const uint32_t sb = sa + kCtaWarps;
+      const bool hasb = sb < nact;
+      uint64_t ya = shoup_mul(vst[sa], Glw, Glq, p);
+      uint64_t yb = shoup_mul(vst[hasb ? sb : sa], Glw, Glq, p);
+      uint32_t s = lane + 1;
+#pragma unroll 1
+      for (uint32_t u = 0;; u++) {
+        if (W.probe_home(ya) && W.probe(ya)) ML.push(ya, sa, s);
+        if (hasb && W.probe_home(yb) && W.probe(yb)) ML.push(yb, sb, s);
+        if (u + 1 >= spl) break;
+        ya = shoup_mul(ya, Gw, Gq, p);
+        yb = shoup_mul(yb, Gw, Gq, p);
+        s += 32;
+      }
+    }
+    __syncthreads();
+
+    // Tag matches: recompute the baby steps and compare full 64-bit values.
+    const uint32_t mc = *ML.count;
+    if (mc > ML.cap) {
+      if (tid == 0) {
+        const uint32_t r = atomicAdd(cb.redo_count, 1u);
+        if (r < cb.cap) cb.redo[r] = i;
+      }
+    } else if (mc > 0) {
+      uint64_t va = Bl, vb = Blb;
+      const uint64_t Stw = rec[kElStw], Stq = rec[kElStq];
+#pragma unroll 1
+      for (uint32_t t = 0; t < CL; t++) {
+#pragma unroll 1
+        for (uint32_t q = 0; q < mc; q++) {
+          const Match mt = ML.list[q];
+          if (mt.y == va || mt.y == vb) {  // both when B has a small order
+            const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+            const uint32_t row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
+            if (mt.y == va) record_hit(J, hb, p, row, mt.s, ja0 + t);
+            if (mt.y == vb) record_hit(J, hb, p, row, mt.s, jb0 + t);
+          }
+        }
+        va = shoup_mul(va, Stw, Stq, p);
+        vb = shoup_mul(vb, Stw, Stq, p);
+      }
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// The exact path: a table of (tag << jbits) | j entries with linear probing per
+// prime, for the primes whose tag matches overflowed the fast path's list.  WG
+// warps share a prime (1 for warp-per-prime jobs, kCtaWarps for CTA jobs) with
+// the same chain layout as the fast kernels.
+template <int WG>
+__global__ void __launch_bounds__(WG == 1 ? 32 * kWarpsPerBlock : 32 * WG, 1)
 bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t G = 32 * WG;                           // threads per prime
+  constexpr uint32_t NG = WG == 1 ? kWarpsPerBlock : 1;     // primes per block
+  const uint32_t grp = threadIdx.x / G, gt = threadIdx.x % G, wig = gt >> 5, lane = threadIdx.x & 31;
   const uint32_t S = 1u << J.exact_log2;
   const uint32_t tmask = S - 1;
-  uint32_t *tab = reinterpret_cast<uint32_t *>(smem4) + (size_t)warp * S;
+  uint32_t *tab = reinterpret_cast<uint32_t *>(smem4) + (size_t)grp * S;
   const uint32_t jbits = J.jbits;
   const uint32_t jmask = (1u << jbits) - 1u;
   const uint32_t tagmask = (1u << (32 - jbits)) - 1u;
   const uint32_t tl = J.exact_log2;
   const uint32_t lane_t = lane & (J.tlanes - 1);
   const uint32_t lane_row = lane / J.tlanes;
+  const uint32_t rows_pass = J.rows_per_it * WG;  // row slots per pass of the group
   const uint32_t rc = *cb.redo_count;
   const uint32_t nr = rc < cb.cap ? rc : cb.cap;
-  const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+  const uint32_t ngroups = gridDim.x * NG;
 #pragma unroll 1
-  for (uint32_t r = blockIdx.x * kWarpsPerBlock + warp; r < nr; r += nwarps) {
+  for (uint32_t r = blockIdx.x * NG + grp; r < nr; r += ngroups) {
     const uint32_t i = cb.redo[r];
     const uint64_t p = rec_el(J, cb, kElP, i), pinv = rec_el(J, cb, kElPinv, i);
     const uint32_t nact = (uint32_t)rec_el(J, cb, kElNact, i);
     const uint64_t Gs = rec_el(J, cb, kElGs, i);
     const uint64_t Stw = rec_el(J, cb, kElStw, i), Stq = rec_el(J, cb, kElStq, i);
-    for (uint32_t q = lane; q < S; q += 32) tab[q] = kEmpty;
-    __syncwarp();
-    // the lane's two baby chains, j = (lane + 32c)*chain_len + t
-    const uint64_t Bl = rec_el(J, cb, J.el_tab + lane, i);
+    if (WG == 1) __syncwarp();
+    else __syncthreads();
+    for (uint32_t q = gt; q < S; q += G) tab[q] = kEmpty;
+    if (WG == 1) __syncwarp();
+    else __syncthreads();
+    // the thread's two baby chains, j = (gt + G*c)*chain_len + t
+    uint64_t Bl = rec_el(J, cb, J.el_tab + lane, i);
+    if (WG > 1 && wig) Bl = shoup_mul(Bl, rec_el(J, cb, kElWoff + 2 * wig, i), rec_el(J, cb, kElWoff + 2 * wig + 1, i), p);
 #pragma unroll 1
     for (uint32_t c = 0; c < 2; c++) {
-      const uint32_t j0 = (lane + 32 * c) * J.chain_len;
+      const uint32_t j0 = (gt + G * c) * J.chain_len;
       uint64_t v = c ? shoup_mul(Bl, rec_el(J, cb, kElOfw, i), rec_el(J, cb, kElOfq, i), p) : Bl;
 #pragma unroll 1
       for (uint32_t j = j0; j < J.m && j < j0 + J.chain_len; j++) {
@@ -891,15 +1048,16 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         v = shoup_mul(v, Stw, Stq, p);
       }
     }
-    __syncwarp();
+    if (WG == 1) __syncwarp();
+    else __syncthreads();
     const uint64_t Gl = rec_el(J, cb, J.el_tab + 32 + lane, i);
-    const uint32_t ngi = (nact + J.rows_per_it - 1) / J.rows_per_it;
+    const uint32_t ngi = (nact + rows_pass - 1) / rows_pass;
 #pragma unroll 1
     for (uint32_t gi = 0; gi < ngi; gi++) {
-      const uint32_t slot = gi * J.rows_per_it + lane_row;
+      const uint32_t slot = gi * rows_pass + wig * J.rows_per_it + lane_row;
       if (slot < nact) {
         const uint32_t row = (uint32_t)(rec_el(J, cb, J.el_row + (slot >> 2), i) >> (16 * (slot & 3))) & 0xffffu;
-        uint64_t y = montmul(rec_el(J, cb, kElV + slot, i), Gl, p, pinv);
+        uint64_t y = montmul(rec_el(J, cb, J.el_v + slot, i), Gl, p, pinv);
         uint32_t s = lane_t + 1;
 #pragma unroll 1
         for (uint32_t u = 0; u < J.steps_per_lane; u++) {
@@ -919,13 +1077,14 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         }
       }
     }
-    __syncwarp();
   }
 }
 
-int bsgs_exact_smem_bytes(const JobDev &job) { return kWarpsPerBlock * (4 << job.exact_log2); }
+int bsgs_exact_smem_bytes(const JobDev &job) {
+  return (job.cta_warps > 1 ? 1 : kWarpsPerBlock) * (4 << job.exact_log2);
+}
 
-static cudaError_t configure_one(const void *fn, int smem, int device, int *grid_out) {
+static cudaError_t configure_one(const void *fn, int smem, int threads, int device, int *grid_out) {
   // The limit is a property of the kernel shared by every job in the process,
   // so it is set to the device maximum (the same value from every thread)
   // rather than to this job's size, which a concurrent job could lower.
@@ -938,7 +1097,7 @@ static cudaError_t configure_one(const void *fn, int smem, int device, int *grid
   e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kWarpsPerBlock, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
   if (e != cudaSuccess) return e;
   int sms = 0;
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -948,21 +1107,37 @@ static cudaError_t configure_one(const void *fn, int smem, int device, int *grid
   return cudaSuccess;
 }
 
+static int bsgs_threads(const JobDev &job) { return job.cta_warps > 1 ? 32 * kCtaWarps : 32 * kWarpsPerBlock; }
+
+static const void *bsgs_fast_fn(const JobDev &job) {
+  return job.cta_warps > 1 ? (const void *)bsgs_cta_kernel : (const void *)bsgs_fn(job.tlanes);
+}
+
+static const void *bsgs_exact_fn(const JobDev &job) {
+  return job.cta_warps > 1 ? (const void *)bsgs_exact_kernel<kCtaWarps> : (const void *)bsgs_exact_kernel<1>;
+}
+
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out) {
-  cudaError_t e = configure_one((const void *)bsgs_fn(job.tlanes), bsgs_smem_bytes(job), device, grid_out);
+  cudaError_t e = configure_one(bsgs_fast_fn(job), bsgs_smem_bytes(job), bsgs_threads(job), device, grid_out);
   if (e != cudaSuccess) return e;
-  return configure_one((const void *)bsgs_exact_kernel, bsgs_exact_smem_bytes(job), device, exact_grid_out);
+  return configure_one(bsgs_exact_fn(job), bsgs_exact_smem_bytes(job), bsgs_threads(job), device, exact_grid_out);
 }
 
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st) {
-  bsgs_fn(job.tlanes)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+  if (job.cta_warps > 1)
+    bsgs_cta_kernel<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+  else
+    bsgs_fn(job.tlanes)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bsgs_exact(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                               cudaStream_t st) {
-  bsgs_exact_kernel<<<grid, 32 * kWarpsPerBlock, bsgs_exact_smem_bytes(job), st>>>(job, cb, hb);
+  if (job.cta_warps > 1)
+    bsgs_exact_kernel<kCtaWarps><<<grid, 32 * kCtaWarps, bsgs_exact_smem_bytes(job), st>>>(job, cb, hb);
+  else
+    bsgs_exact_kernel<1><<<grid, 32 * kWarpsPerBlock, bsgs_exact_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();
 }
 
