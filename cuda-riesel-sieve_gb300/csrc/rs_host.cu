@@ -283,8 +283,9 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
           const uint64_t wsm = align_up((20u << blog) + 16 * (stage * 8 <= 2048 ? stage : kElV) + 16 * kMatchCap + 16, 16);
           const double cta_bytes = (double)align_up(4 * wsm, 128) + 1024.0;
           const double warps = std::min(kFullWarps, 4.0 * std::floor(kSmemPerSm / cta_bytes));
-          if (warps >= 4) {
-            const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+          const double fp = ER * (double)T * ((double)m / nb) / 65536.0;  // expected tag matches per prime
+          // (a prime with more than kMatchCap matches takes the slow exact path)
+          if (warps >= 4 && fp <= 2.0) {
             const double cost = (std::ceil((double)m / 32.0) + kGiantWeight * std::ceil(ER / rpi) * spl +
                                  nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
                                 std::sqrt(kFullWarps / warps);
@@ -299,8 +300,8 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
         const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((m + 1) / 2));  // <= 2 entries per bucket
         const double nb = (double)(1u << blog);
         const double smem = 20.0 * nb + 8.0 * (rows + 2) + 16.0 * (kCtaMatchCap + 1);
-        if (m <= mcap && m * T >= X && slog <= 15 && smem <= 232448.0) {
-          const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+        const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+        if (m <= mcap && m * T >= X && slog <= 15 && smem <= 232448.0 && fp <= 16.0) {
           const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
                                nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
                               std::sqrt(kFullWarps / kCtaWarps);
