@@ -293,7 +293,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
           }
         }
       }
-      if (T >= 32) {  // a CTA per prime: 64 * kCtaWarps chains share a table of up to ~160 KB
+      if (T >= 32 && T <= 256) {  // a CTA per prime: 64 * kCtaWarps chains share a table of up to ~160 KB
         const uint64_t chains = 64 * kCtaWarps;
         const uint64_t m = (m0 + chains - 1) / chains * chains;
         const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));

@@ -940,25 +940,42 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
       __syncthreads();
     }
 
-    // Giant steps: warp w takes row slots w, w + W, ... two at a time
+    // Giant steps: warp w takes row slots w, w + W, ..., four at a time (four
+    // independent product chains per lane).  The loop tests home buckets only
+    // and records the outcome as bits (step u of slot k -> bit 4u + k, spl <= 8);
+    // tag hits and full buckets are finished after each pass.
     const uint64_t Glm = rec[J.el_tab + 32 + lane];
     const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
     const uint64_t Gw = rec[kElGw], Gq = rec[kElGq];
 #pragma unroll 1
-    for (uint32_t sa = warp; sa < nact; sa += 2 * kCtaWarps) {
-      const uint32_t sb = sa + kCtaWarps;
-      const bool hasb = sb < nact;
-      uint64_t ya = shoup_mul(vst[sa], Glw, Glq, p);
-      uint64_t yb = shoup_mul(vst[hasb ? sb : sa], Glw, Glq, p);
-      uint32_t s = lane + 1;
+    for (uint32_t s0 = warp; s0 < nact; s0 += 4 * kCtaWarps) {
+      uint64_t y[4];
+      uint32_t valid = 0;
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++) {
+        const uint32_t sl = s0 + k * kCtaWarps;
+        valid |= (sl < nact ? 0x11111111u : 0u) << k;
+        y[k] = shoup_mul(vst[sl < nact ? sl : s0], Glw, Glq, p);
+      }
+      uint32_t bits = 0;
 #pragma unroll 1
       for (uint32_t u = 0;; u++) {
-        if (W.probe_home(ya) && W.probe(ya)) ML.push(ya, sa, s);
-        if (hasb && W.probe_home(yb) && W.probe(yb)) ML.push(yb, sb, s);
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++)
+          if (W.probe_home(y[k])) bits |= 1u << (4 * u + k);
         if (u + 1 >= spl) break;
-        ya = shoup_mul(ya, Gw, Gq, p);
-        yb = shoup_mul(yb, Gw, Gq, p);
-        s += 32;
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++) y[k] = shoup_mul(y[k], Gw, Gq, p);
+      }
+      bits &= valid;
+      while (bits) {  // rare
+        const uint32_t b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t k = b & 3, u = b >> 2, sl = s0 + k * kCtaWarps;
+        uint64_t v = shoup_mul(vst[sl], Glw, Glq, p);
+#pragma unroll 1
+        for (uint32_t q = 0; q < u; q++) v = shoup_mul(v, Gw, Gq, p);
+        if (W.probe(v)) ML.push(v, sl, lane + 1 + 32 * u);
       }
     }
     __syncthreads();
