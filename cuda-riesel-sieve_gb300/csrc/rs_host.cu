@@ -828,6 +828,7 @@ int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   info->primes_per_launch = j->cb.cap;
   info->work_per_prime = pl.work_per_prime;
   info->upload_bytes = j->job_bytes;
+  info->warps_per_prime = pl.cta ? kCtaWarps : 1;
   return RS_OK;
 }
 
@@ -1111,6 +1112,7 @@ extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp
   info->giant_steps = pl.T;
   info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
   info->work_per_prime = pl.work_per_prime;
+  info->warps_per_prime = pl.cta ? kCtaWarps : 1;
   return RS_OK;
 }
 

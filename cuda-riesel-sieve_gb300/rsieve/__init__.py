@@ -74,6 +74,8 @@ class JobInfo(ctypes.Structure):
         ("primes_per_launch", ctypes.c_uint32),
         ("work_per_prime", ctypes.c_double),
         ("upload_bytes", ctypes.c_uint64),
+        ("warps_per_prime", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

@@ -87,6 +87,8 @@ typedef struct {
   uint32_t primes_per_launch;
   double work_per_prime; /* algorithmic montmuls per prime: 2*sqrt(E[R]*X) */
   uint64_t upload_bytes; /* host->device bytes copied when the job was created */
+  uint32_t warps_per_prime; /* 1: a warp per prime; 16: a CTA per prime (large tables) */
+  uint32_t reserved;
 } rs_job_info;
 
 /* Counters and device-timed durations of the last rs_sieve_range call. */

@@ -126,3 +126,19 @@ def test_abcd_remove_round_trip(rs, oracle_mod, sr745_text):
     # nothing removed: identical candidate sets
     job3 = oracle_mod.Job.from_abcd(rs.abcd_remove(sr745_text, [], 1))
     assert all(np.array_equal(job3.nlist(i), job.nlist(i)) for i in range(len(ks)))
+
+
+def test_plan_layouts(rs):
+    """The planner keeps the warp-per-prime layout for the plain job and picks a
+    CTA per prime for the wide job, whose best table does not fit a warp."""
+    import rsieve.synth as S
+
+    d = rs.plan_abcd(S.to_abcd(*S.plain_job(1)))
+    assert (d["Q"], d["baby_steps"], d["giant_steps"], d["warps_per_prime"]) == (2, 1152, 32, 1)
+    # the wide job's shape (b=2, 1000 k, n in [1e6, 3e6]) at a lower density: same rows and plan
+    d = rs.plan_abcd(S.to_abcd(*S.make_job(1, 2, 1000, 3, 10**7, 10**6, 3 * 10**6, 0.001)))
+    assert d["warps_per_prime"] == 16 and d["baby_steps"] % 1024 == 0
+    assert d["baby_steps"] * d["giant_steps"] >= d["x_range"]
+    # expected false tag matches per prime stay well inside the CTA match list
+    er = d["rows"] * (0.5 if d["Q"] % 2 == 0 else 0.75)
+    assert er * d["giant_steps"] * d["baby_steps"] / (d["table_slots"] / 8) / 65536 <= 16
