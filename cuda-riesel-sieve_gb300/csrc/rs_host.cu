@@ -208,7 +208,7 @@ static int count_rows(const Seqs &s, uint32_t Q, bool datless) {
   return rows;
 }
 
-static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
+static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_bitmap = true) {
   uint32_t nmin = 0xffffffffu, nmax = 0, ncand = 0;
   for (auto &v : s.n) {
     if (v.empty()) continue;
@@ -338,7 +338,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl) {
         pl.row_r.push_back(r);
         pl.row_kidx.push_back((uint32_t)i);
       }
-    if (!datless) {
+    if (!datless && with_bitmap) {
       // candidate bitmap rows (bits for x - x_lo)
       size_t base_words = pl.bitmap.size();
       size_t nr = pl.row_r.size() - pl.k_row0[i];
@@ -1096,7 +1096,7 @@ extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp
   if (optp) opt = *optp;
   else rs_options_default(&opt);
   Plan pl;
-  rc = make_plan(s, opt, pl);
+  rc = make_plan(s, opt, pl, false);  // the plan's parameters only
   if (rc) return rc;
   memset(info, 0, sizeof(*info));
   info->base = s.base;
