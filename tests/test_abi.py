@@ -135,8 +135,9 @@ def test_plan_layouts(rs):
 
     d = rs.plan_abcd(S.to_abcd(*S.plain_job(1)))
     assert (d["Q"], d["baby_steps"], d["giant_steps"], d["warps_per_prime"]) == (2, 1152, 32, 1)
-    # the wide job's shape: b=2, 1000 k, both residues mod 2 of n in [1e6, 3e6] (2000 rows)
-    wide = "".join(f"ABCD {k}*2^$a-1 [1000000]\n1\n1999999\n" for k in range(3, 2003, 2))
+    # the wide job's shape: b=2, 1000 k, n in [1e6, 3e6] with every residue mod Q <= 48
+    body = "\n".join(["1"] * 47 + [str(3 * 10**6 - 10**6 - 47)])
+    wide = "".join(f"ABCD {k}*2^$a-1 [1000000]\n{body}\n" for k in range(3, 2003, 2))
     d = rs.plan_abcd(wide)
     assert d["warps_per_prime"] == 16 and d["baby_steps"] % 1024 == 0
     assert d["baby_steps"] * d["giant_steps"] >= d["x_range"]
