@@ -53,11 +53,27 @@ SLICE = 10**10
 MONTMUL_MULS = 19  # 32-bit multiply-class PTX instructions per 64-bit Montgomery product
 WORKLOAD = ("plain_steady: b=745, 22 seeded odd k in [3,1e6], n in [180000,250000] at 5% density, "
             "all primes p in [1e13, 1e13+1e11)")
+JOB = "plain_job"
+
+# --workload wide: the wide-n, many-k job near 2^50 (a parity configuration,
+# measured on request; the default line is the plain steady-state workload)
+WIDE = {
+    "METRIC": "p/sec (b=2, 1000 k, n 1e6–3e6)", "P_START": 1 << 50, "WINDOW": 5 * 10**10, "SLICE": 5 * 10**9,
+    "WORKLOAD": ("wide: b=2, 1000 seeded odd k in [3,1e7], n in [1e6,3e6] at 2% density, "
+                 "all primes p in [2^50, 2^50+5e10)"),
+    "JOB": "wide_job", "PROFILE": "bsgs_cta_kernel.wide.txt",
+}
+PROFILE = "bsgs_kernel.plain_steady.txt"  # committed ncu summary with the BSGS kernel's DRAM bytes per prime
+
+
+def select_workload(name: str) -> None:
+    if name == "wide":
+        globals().update(WIDE)
 
 
 def bsgs_bytes_per_prime():
     """DRAM bytes per prime of the BSGS kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "bsgs_kernel.plain_steady.txt")
+    path = os.path.join(ROOT, "profiles", PROFILE)
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_prime:"):
@@ -184,7 +200,7 @@ def cpu_baseline(job_args, seconds: float = 12.0) -> dict:
     f, npr = oj.sieve(P_START + w0, P_START + w0 + width - 1, threads=threads)
     dt = time.perf_counter() - t
     return {"value": width / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"p in [1e13+{w0}, +{width}) ({npr} primes, {len(f)} factors), {dt:.1f} s"}
+            "sample": f"p in [{P_START}+{w0}, +{width}) ({npr} primes, {len(f)} factors), {dt:.1f} s"}
 
 
 def run_reference(args, rank: int) -> None:
@@ -197,7 +213,7 @@ def run_reference(args, rank: int) -> None:
     import rsieve.synth as S
 
     oracle.build()
-    b, s, ks, nl = S.plain_job(1)
+    b, s, ks, nl = getattr(S, JOB)(1)
     oj = oracle.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
     threads = oracle.default_threads()
     # per-step sample sized to ~3 s of CPU work
@@ -219,7 +235,7 @@ def run_reference(args, rank: int) -> None:
         a += width
     dt = time.perf_counter() - t
     value = args.steps * width / dt
-    sample = (f"{args.steps} steps of {width}-wide windows of the workload from 1e13 "
+    sample = (f"{args.steps} steps of {width}-wide windows of the workload from {P_START} "
               f"({tot_p} primes, {tot_f} factors)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -342,10 +358,11 @@ def run_served(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--workload", default="plain", choices=["plain", "wide"])
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--slice", type=float, default=SLICE)
+    ap.add_argument("--slice", type=float, default=None, help="p-width of one step (default: the workload's)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--Q", type=int, default=0, help="force the subsequence modulus (default: planner)")
@@ -358,6 +375,9 @@ def main() -> None:
     ap.add_argument("--served-loads", type=float, nargs="*", default=[0.5, 1.0, 1.5])
     ap.add_argument("--slots", type=int, default=4, help="jobs running at once in the served form")
     args = ap.parse_args()
+    select_workload(args.workload)
+    if args.slice is None:
+        args.slice = SLICE
     if args.served:
         run_served(args)
         return
@@ -375,7 +395,7 @@ def main() -> None:
     dist = Dist(world, local, "nccl")
     dev = local
     slice_w = int(args.slice)
-    job_args = S.plain_job(1)
+    job_args = getattr(S, JOB)(1)
     b, s, ks, nl = job_args
     abcd = S.to_abcd(b, s, ks, nl)
 
@@ -455,9 +475,9 @@ def main() -> None:
         "config": {
             "workload": WORKLOAD, "slice_width": slice_w, "plan": {
                 k: info[k] for k in ("Q", "rows", "x_range", "baby_steps", "giant_steps", "table_slots",
-                                     "primes_per_launch")},
-            "l2": "no flush: each step streams ~2.7 GB of fresh prime windows (> 129 MB L2); the 0.2 MB "
-                  "job tables stay resident by design",
+                                     "primes_per_launch", "warps_per_prime")},
+            "l2": ("no flush: each step streams the per-prime records of a fresh prime window (GBs, > 129 MB L2); "
+                   "the job tables stay resident by design"),
             "parallelism": f"p-range shards x{world}, no collective",
         },
         "roofline": {

@@ -465,7 +465,7 @@ static int upload_job(rs_job *j) {
   const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
   const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
   // Quadratic-character tables, one per distinct odd part > 1 of k and b,
-  // built on the device when they fit in 256 MB.
+  // built on the device when they fit in 1 GB (about 60 ms of build time).
   std::vector<uint32_t> tab_k, tab_off;  // odd parts and their word offsets
   std::vector<uint32_t> kjac(nk, kNoTable);
   uint32_t bjac = kNoTable;
@@ -484,7 +484,7 @@ static int upload_job(rs_job *j) {
     };
     for (uint32_t i = 0; i < nk; i++) kjac[i] = find_or_add(kodd[i]);
     bjac = find_or_add(bo);
-    if (twords > (64ull << 20)) {  // too large: compute the symbols instead
+    if (twords > (256ull << 20)) {  // too large: compute the symbols instead
       std::fill(kjac.begin(), kjac.end(), kNoTable);
       bjac = kNoTable;
       tab_k.clear();

@@ -990,6 +990,8 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
     } else if (mc > 0) {
       uint64_t va = Bl, vb = Blb;
       const uint64_t Stw = rec[kElStw], Stq = rec[kElStq];
+      const uint32_t bq = J.bq_small, rcp = (uint32_t)rec[kElRcp];
+      const bool small = cb.small_step != 0;
 #pragma unroll 1
       for (uint32_t t = 0; t < CL; t++) {
 #pragma unroll 1
@@ -1002,8 +1004,8 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
             if (mt.y == vb) record_hit(J, hb, p, row, mt.s, jb0 + t);
           }
         }
-        va = shoup_mul(va, Stw, Stq, p);
-        vb = shoup_mul(vb, Stw, Stq, p);
+        va = small ? mul_small(va, bq, rcp, p) : shoup_mul(va, Stw, Stq, p);
+        vb = small ? mul_small(vb, bq, rcp, p) : shoup_mul(vb, Stw, Stq, p);
       }
     }
   }
