@@ -93,6 +93,19 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
     while (z > a && (text[z - 1] == '\r' || text[z - 1] == ' ' || text[z - 1] == '\t')) z--;
     while (a < z && (text[a] == ' ' || text[a] == '\t')) a++;
     if (a == z) continue;
+    if (text[a] >= '0' && text[a] <= '9' && z - a <= 10 && !out.k.empty()) {
+      // the common line: a plain decimal n delta, parsed in place
+      uint64_t d = 0;
+      size_t c = a;
+      for (; c < z && text[c] >= '0' && text[c] <= '9'; c++) d = d * 10 + (uint64_t)(text[c] - '0');
+      if (c == z) {
+        if (d == 0) return fail(RS_ERR_INVALID, "ABCD line %ld: bad n delta", line);
+        total += d;
+        if (total > 0x7fffffffull) return fail(RS_ERR_INVALID, "ABCD line %ld: n exceeds 2^31-1", line);
+        out.n.back().push_back((uint32_t)total);
+        continue;
+      }
+    }
     std::string s(text + a, z - a);
     if (s.compare(0, 4, "ABCD") == 0 && s.size() > 4 && (s[4] == ' ' || s[4] == '\t')) {
       const char *c = s.c_str() + 5;
@@ -160,6 +173,8 @@ static void normalise(Seqs &s) {
     }
   }
   for (auto &v : o.n) {
+    if (std::adjacent_find(v.begin(), v.end(), [](uint32_t x, uint32_t y) { return x >= y; }) == v.end())
+      continue;  // already strictly increasing (positive deltas)
     std::sort(v.begin(), v.end());
     v.erase(std::unique(v.begin(), v.end()), v.end());
   }
@@ -199,11 +214,14 @@ static int count_rows(const Seqs &s, uint32_t Q, bool datless) {
   std::vector<char> seen(Q);
   for (size_t i = 0; i < s.k.size(); i++) {
     std::fill(seen.begin(), seen.end(), 0);
-    for (uint32_t n : s.n[i])
+    uint32_t got = 0;
+    for (uint32_t n : s.n[i]) {
       if (!seen[n % Q]) {
         seen[n % Q] = 1;
-        rows++;
+        if (++got == Q) break;  // every residue present: the rest of the list adds nothing
       }
+    }
+    rows += (int)got;
   }
   return rows;
 }
