@@ -34,6 +34,8 @@ static void usage() {
   printf("-v       : Don't verify: report every n in [nmin,nmax] (datless).\n");
   printf("-w FILE  : After sieving, write FILE: the input ABCD without the candidates whose\n");
   printf("           factors are in the factor file, headers marked \"// Sieved to P1\".\n");
+  printf("-A       : Autotune: time the cheapest plans of the cost model on the first part of the\n");
+  printf("           range and keep the fastest (replaces hand-tuning -Q/-m/-b/-t).\n");
   printf("-C FILE  : Checkpoint: resume from the p recorded in FILE (if it is for the same\n");
   printf("           input and P1) and record progress there after every block of launches.\n");
   printf("-h       : Prints this help\n");
@@ -49,7 +51,8 @@ int main(int argc, char **argv) {
   bool scale_given = false;
   int inp;
   const char *abcd_out = nullptr, *ckpt = nullptr;
-  while ((inp = getopt(argc, argv, "b:hi:m:p:P:Q:O:s:t:vw:C:")) != -1) {
+  bool autotune = false;
+  while ((inp = getopt(argc, argv, "Ab:hi:m:p:P:Q:O:s:t:vw:C:")) != -1) {
     switch (inp) {
       case 'b': block_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
       case 't': thread_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
@@ -72,6 +75,7 @@ int main(int argc, char **argv) {
       case 'v': opt.datless = 1; opt.host_verify = 1; break;
       case 'w': abcd_out = optarg; break;
       case 'C': ckpt = optarg; break;
+      case 'A': autotune = true; break;
       default: return 0;
     }
   }
@@ -123,6 +127,21 @@ int main(int argc, char **argv) {
   printf("Q=%u. Rows=%u. Range=%u. Baby steps=%u. Giant steps=%u. Table slots=%u. Primes per launch=%u\n\n",
          info.Q, info.rows, info.x_range, info.baby_steps, info.giant_steps, info.table_slots,
          info.primes_per_launch);
+
+  if (autotune) {
+    // a sample of about four launches' worth of primes at the start of the range
+    const double lp = std::log((double)std::max(low, 16ull));
+    const unsigned long long w = (unsigned long long)(4.0 * info.primes_per_launch * lp);
+    const unsigned long long hi = (high - low < w) ? high : low + w - 1;
+    rc = rs_job_autotune(job, low, hi, 3, &info);
+    if (rc) {
+      fprintf(stderr, "error: %s\n", rs_last_error());
+      rs_job_destroy(job);
+      return 1;
+    }
+    printf("Autotuned on [%llu, %llu]: Q=%u. Baby steps=%u. Giant steps=%u. Warps per prime=%u\n\n", low, hi,
+           info.Q, info.baby_steps, info.giant_steps, info.warps_per_prime);
+  }
 
   // Resume from a checkpoint of the same input and P1.
   unsigned long long p = low;

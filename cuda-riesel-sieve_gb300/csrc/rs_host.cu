@@ -226,7 +226,17 @@ static int count_rows(const Seqs &s, uint32_t Q, bool datless) {
   return rows;
 }
 
-static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_bitmap = true) {
+// One point of the planner's search: the parameters that define a plan, and its modelled cost.
+struct PlanChoice {
+  uint32_t Q = 0, T = 0, m = 0;
+  bool cta = false;
+  double cost = 0;
+};
+
+// Plan a job.  With `force`, take exactly that choice (it must be feasible);
+// with `ranked`, also return every feasible choice, cheapest first.
+static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_bitmap = true,
+                     const PlanChoice *force = nullptr, std::vector<PlanChoice> *ranked = nullptr) {
   uint32_t nmin = 0xffffffffu, nmax = 0, ncand = 0;
   for (auto &v : s.n) {
     if (v.empty()) continue;
@@ -255,12 +265,22 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
   // A giant step (Shoup product + probe) costs about 1.4 baby steps (a short or
   // Shoup product + insert), measured on the benchmark job.
   constexpr double kGiantWeight = 1.4;
+  // Setup-kernel cost per (k, n mod Q) row, in the same units.
+  constexpr double kRowCost = 0.18;
+  // A step of the CTA kernel costs more than one of the warp kernel (block-wide
+  // barriers, per-prime tag-match passes); fitted with rs_job_autotune on mixed jobs.
+  constexpr double kCtaStepCost = 1.25;
   double best = 1e300;
   for (uint32_t Q : Qs) {
     const uint32_t X = nmax / Q - nmin / Q + 1;
     const int rows = count_rows(s, Q, datless);
     const double ER = rows * ((Q & 1) ? 0.75 : 0.5);
     auto consider = [&](bool cta, uint64_t T, uint64_t m, uint32_t blog, uint32_t slog, double cost) {
+      if (ranked) ranked->push_back(PlanChoice{Q, (uint32_t)T, (uint32_t)m, cta, cost});
+      if (force) {
+        if (force->Q != Q || force->T != T || force->m != m || force->cta != cta) return;
+        cost = -1.0;  // the forced choice wins
+      }
       if (cost < best) {
         best = cost;
         pl.Q = Q;
@@ -305,7 +325,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
           // (a prime with more than kMatchCap matches takes the slow exact path)
           if (warps >= 4 && fp <= 2.0) {
             const double cost = (std::ceil((double)m / 32.0) + kGiantWeight * std::ceil(ER / rpi) * spl +
-                                 nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
+                                 nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
                                 std::sqrt(kFullWarps / warps);
             consider(false, T, m, blog, slog, cost);
           }
@@ -321,13 +341,15 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
         const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
         if (m <= mcap && m * T >= X && slog <= 15 && smem <= 232448.0 && fp <= 16.0) {
           const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
-                               nb * 8 / 1024.0 + 3.7 + 0.062 * rows + std::min(1.0, fp) * (double)m / 32.0) *
-                              std::sqrt(kFullWarps / kCtaWarps);
+                               nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
+                              std::sqrt(kFullWarps / kCtaWarps) * kCtaStepCost;
           consider(true, T, m, blog, slog, cost);
         }
       }
     }
   }
+  if (ranked)
+    std::sort(ranked->begin(), ranked->end(), [](const PlanChoice &a, const PlanChoice &b) { return a.cost < b.cost; });
   if (pl.Q == 0) return fail(RS_ERR_INVALID, "no feasible plan (n range too wide for the -m limit)");
   pl.nmin = nmin;
   pl.nmax = nmax;
@@ -399,6 +421,7 @@ struct DevPrimes {
 
 struct rs_job {
   std::mutex mu;
+  std::vector<PlanChoice> ranked;  // the planner's feasible choices, cheapest first (for rs_job_autotune)
   std::shared_ptr<DevPrimes> primes;  // sieving primes in use (d_sp, d_sp_rcp below point into it)
   rs_options opt;
   Seqs seqs;
@@ -717,7 +740,8 @@ static void free_job(rs_job *j) {
   delete j;
 }
 
-static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out) {
+static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out,
+                            const PlanChoice *force = nullptr) {
   if (!out) return fail(RS_ERR_INVALID, "job pointer is NULL");
   *out = nullptr;
   rs_options opt;
@@ -730,11 +754,13 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out) {
   if (opt.block_scale < 0 || opt.block_scale > 31 || opt.thread_scale < 0 || opt.thread_scale > 31)
     return fail(RS_ERR_INVALID, "-b/-t scale must be in [1, 31]");
   Plan pl;
-  int rc = make_plan(seqs, opt, pl);
+  std::vector<PlanChoice> ranked;
+  int rc = make_plan(seqs, opt, pl, true, force, &ranked);
   if (rc) return rc;
   rc = check_device(opt.device);
   if (rc) return rc;
   rs_job *j = new rs_job();
+  j->ranked = std::move(ranked);
   j->opt = opt;
   j->seqs = std::move(seqs);
   j->plan = std::move(pl);
@@ -1089,6 +1115,83 @@ extern "C" int rs_sieve_range(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *ou
     if (rc != kRetryHits) return rc;
   }
   return fail(RS_ERR_INTERNAL, "candidate-hit buffer overflow could not be resolved");
+}
+
+// Exchange everything but the mutex (and the ranked choices, which belong to the job's input).
+static void swap_job_state(rs_job *a, rs_job *b) {
+  std::swap(a->primes, b->primes);
+  std::swap(a->opt, b->opt);
+  std::swap(a->plan, b->plan);
+  std::swap(a->dev, b->dev);
+  std::swap(a->device, b->device);
+  std::swap(a->st, b->st);
+  std::swap(a->d_job, b->d_job);
+  std::swap(a->job_bytes, b->job_bytes);
+  std::swap(a->sp_limit, b->sp_limit);
+  std::swap(a->nsp, b->nsp);
+  std::swap(a->nsp_small, b->nsp_small);
+  std::swap(a->d_gbits, b->d_gbits);
+  std::swap(a->gbits_words, b->gbits_words);
+  std::swap(a->d_sp, b->d_sp);
+  std::swap(a->d_sp_rcp, b->d_sp_rcp);
+  std::swap(a->cb, b->cb);
+  std::swap(a->d_chunk, b->d_chunk);
+  std::swap(a->hb, b->hb);
+  std::swap(a->d_hits, b->d_hits);
+  std::swap(a->h_counts, b->h_counts);
+  std::swap(a->h_counts_cap, b->h_counts_cap);
+  std::swap(a->bsgs_grid, b->bsgs_grid);
+  std::swap(a->exact_grid, b->exact_grid);
+  std::swap(a->chunk_cap, b->chunk_cap);
+}
+
+extern "C" int rs_job_autotune(rs_job *j, uint64_t p0, uint64_t p1, uint32_t candidates, rs_job_info *chosen) {
+  if (!j) return fail(RS_ERR_INVALID, "NULL job");
+  if (candidates == 0) candidates = 3;
+  std::lock_guard<std::mutex> lock(j->mu);
+  // distinct layouts among the cheapest modelled choices (the job's own plan is the first)
+  std::vector<PlanChoice> cand;
+  for (const PlanChoice &c : j->ranked) {
+    bool dup = false;
+    for (const PlanChoice &d : cand) dup |= d.Q == c.Q && d.T == c.T && d.m == c.m && d.cta == c.cta;
+    if (!dup) cand.push_back(c);
+    if (cand.size() >= candidates) break;
+  }
+  std::vector<rs_factor> out(1 << 16);
+  double best_ms = 0;
+  size_t best_i = 0;
+  for (size_t c = 0; c < cand.size(); c++) {
+    rs_job *t = nullptr;
+    int rc;
+    if (c == 0) {
+      t = j;
+    } else {
+      Seqs copy = j->seqs;
+      rc = create_from_seqs(std::move(copy), &j->opt, &t, &cand[c]);
+      if (rc) return rc;
+    }
+    rs_stats st{};
+    size_t cnt = 0;
+    rc = RS_OK;
+    for (int attempt = 0; attempt < 4; attempt++) {
+      rc = sieve_range_impl(t, p0, p1, out.data(), out.size(), &cnt, &st);
+      if (rc != kRetryHits) break;
+    }
+    if (rc == RS_ERR_CAPACITY) rc = RS_OK;  // the timing is what counts here
+    if (rc) {
+      if (t != j) free_job(t);
+      return rc;
+    }
+    if (c == 0 || st.gpu_ms < best_ms) {
+      if (c > 0) swap_job_state(j, t);  // the faster plan moves into the caller's job
+      best_ms = st.gpu_ms;
+      best_i = c;
+    }
+    if (t != j) free_job(t);
+  }
+  (void)best_i;
+  if (chosen) return rs_job_info_get(j, chosen);
+  return RS_OK;
 }
 
 extern "C" int rs_write_factors(const rs_job *j, const char *path, const rs_factor *f, size_t count) {

@@ -32,7 +32,7 @@ EXPORTS = (
     "rs_plan_abcd", "rs_job_destroy", "rs_sieve_range", "rs_write_factors", "rs_gpu_primes",
     "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
     "rs_abcd_remove", "rs_server_options_default", "rs_server_create", "rs_server_submit",
-    "rs_server_wait", "rs_server_destroy",
+    "rs_server_wait", "rs_server_destroy", "rs_job_autotune",
 )
 
 
@@ -156,6 +156,7 @@ def lib():
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
         L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
         L.rs_abcd_remove.argtypes = [ctypes.c_char_p, sz, vp, sz, u64, vp, sz, ctypes.POINTER(sz)]
+        L.rs_job_autotune.argtypes = [vp, u64, u64, u32, ctypes.POINTER(JobInfo)]
         L.rs_server_options_default.argtypes = [ctypes.POINTER(ServerOptions)]
         L.rs_server_options_default.restype = None
         L.rs_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
@@ -234,6 +235,13 @@ class Job:
                 continue
             _check(rc)
             return out[: cnt.value], st.as_dict()
+
+    def autotune(self, p0: int, p1: int, candidates: int = 3) -> dict:
+        """Time the cheapest modelled layouts on [p0, p1], keep the fastest; returns the new plan."""
+        info = JobInfo()
+        _check(lib().rs_job_autotune(self._h, p0, p1, candidates, ctypes.byref(info)))
+        self.info = info.as_dict()
+        return self.info
 
     def write_factors(self, path: str, factors) -> None:
         f = np.ascontiguousarray(factors, dtype=FACTOR_DTYPE)

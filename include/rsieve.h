@@ -133,6 +133,16 @@ int rs_job_destroy(rs_job *job);
 int rs_sieve_range(rs_job *job, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
                    size_t *count, rs_stats *stats);
 
+/* Measured autotuning (the reference has hand-set -b/-m/-s/-Q instead): sieve
+ * [p0, p1] with each of the `candidates` (0: 3) cheapest layouts of the
+ * planner's cost model (subsequence modulus Q, baby steps m, giant steps T,
+ * warp or CTA per prime) and keep the fastest by device time for all later
+ * calls.  The window should be representative of the job's range, large
+ * enough to fill a few launches, and is not reported: sieve it again for its
+ * factors, which are the same under every layout.  *chosen (may be NULL)
+ * receives the resulting plan. */
+int rs_job_autotune(rs_job *job, uint64_t p0, uint64_t p1, uint32_t candidates, rs_job_info *chosen);
+
 /* Append factors in the reference's format "%llu | %d*%d^%d-1\n"
  * (kernel_v0.24.6.cu:1830-1835; "+1" for a Sierpinski job). */
 int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, size_t count);

@@ -200,3 +200,21 @@ def test_batch_shaped_jobs(rs, oracle_mod, i):
     assert g == o and len(o) > 0
     g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 3 * 10**5, datless=True)
     assert g == o and st["primes"] > 1000
+
+
+def test_autotune_keeps_results(rs):
+    """Measured autotuning picks one of the cost model's cheapest layouts and
+    leaves the factor set unchanged."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    lo, hi = 10**9, 102 * 10**7 - 1  # the small workload, which has factors
+    with rs.Job(base=b, sign=s, ks=ks, nlists=nl) as j:
+        want, _ = j.sieve(lo, hi)
+    with rs.Job(base=b, sign=s, ks=ks, nlists=nl) as j:
+        before = dict(j.info)
+        info = j.autotune(10**13, 10**13 + 3 * 10**8, candidates=3)
+        got, _ = j.sieve(lo, hi)
+    assert _set(got) == _set(want) and len(want) > 0
+    assert info["Q"] >= 1 and info["baby_steps"] * info["giant_steps"] >= info["x_range"]
+    assert info["num_candidates"] == before["num_candidates"]
