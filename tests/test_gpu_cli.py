@@ -73,3 +73,19 @@ def test_cli_checkpoint_resume_and_abcd_update(rs, oracle_mod, tmp_path):
     cand = {(int(k), int(n)) for k, ns in zip(ks, nl) for n in ns}
     left = {(k, int(n)) for i, k in enumerate(oj2.ks) for n in oj2.nlist(i)}
     assert left == cand - removed
+
+
+def test_cli_autotune_same_factors(rs, tmp_path):
+    """-A picks a layout by measurement; the factor file is the same as without it."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(4)
+    (tmp_path / "job.abcd").write_text(S.to_abcd(b, s, ks, nl))
+    lo, hi = 10**9, 10**9 + 20 * 10**6
+    base = [rs.CLI, "-i", "job.abcd", "-p", str(lo), "-P", str(hi)]
+    r1 = subprocess.run(base + ["-O", "plain.txt"], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    r2 = subprocess.run(base + ["-A", "-O", "tuned.txt"], capture_output=True, text=True, cwd=tmp_path, timeout=300)
+    assert r1.returncode == 0 and r2.returncode == 0, (r1.stderr, r2.stderr)
+    assert "Autotuned on [" in r2.stdout
+    assert sorted(_factors(tmp_path / "plain.txt")) == sorted(_factors(tmp_path / "tuned.txt"))
+    assert _factors(tmp_path / "plain.txt")
