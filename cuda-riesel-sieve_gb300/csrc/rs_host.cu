@@ -533,7 +533,8 @@ static int upload_job(rs_job *j) {
       twords = 0;
     }
   }
-  const size_t o_kj = sec(nk * 4), o_tk = sec(tab_k.size() * 4), o_to = sec(tab_off.size() * 4);
+  const size_t o_kj = sec(nk * 4), o_ki = sec(nk * sizeof(KInfo)), o_tk = sec(tab_k.size() * 4);
+  const size_t o_to = sec(tab_off.size() * 4);
   const size_t o_jb = sec(twords * 4);
   j->job_bytes = o_jb;  // bytes uploaded (the character tables are built on the device)
   std::vector<uint8_t> host(o_jb, 0);
@@ -546,6 +547,22 @@ static int upload_job(rs_job *j) {
   memcpy(host.data() + o_k0, pl.k_row0.data(), (nk + 1) * 4);
   memcpy(host.data() + o_bm, pl.bitmap.data(), pl.bitmap.size() * 4);
   memcpy(host.data() + o_kj, kjac.data(), nk * 4);
+  {
+    std::vector<KInfo> ki(nk);
+    for (uint32_t i = 0; i < nk; i++) {
+      ki[i].k_odd = kodd[i];
+      ki[i].k_e2 = ke2[i];
+      ki[i].k_jac = kjac[i];
+      ki[i].k_val = s.k[i];
+      ki[i].row0 = pl.k_row0[i];
+      ki[i].k_rcp = krcp[i];
+      uint32_t mask = 0;
+      if (pl.Q <= 32)
+        for (uint32_t row = pl.k_row0[i]; row < pl.k_row0[i + 1]; row++) mask |= 1u << pl.row_r[row];
+      ki[i].rmask = mask;
+    }
+    memcpy(host.data() + o_ki, ki.data(), nk * sizeof(KInfo));
+  }
   memcpy(host.data() + o_tk, tab_k.data(), tab_k.size() * 4);
   memcpy(host.data() + o_to, tab_off.data(), tab_off.size() * 4);
   CUDA_TRY(cudaMallocAsync(&j->d_job, off, j->st));
@@ -608,6 +625,7 @@ static int upload_job(rs_job *j) {
   d.bitmap = (const uint32_t *)(b + o_bm);
   d.jac_bits = (const uint32_t *)(b + o_jb);
   d.k_jac = (const uint32_t *)(b + o_kj);
+  d.kinfo = (const KInfo *)(b + o_ki);
   d.b_jac = bjac;
   uint32_t bb = s.base, be = 0;
   while (!(bb & 1)) {

@@ -46,6 +46,14 @@ constexpr uint32_t kElV = 12;      // V in the warp-per-prime layout (W == 1)
 constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
 constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
+// Per-k data of the setup kernel's row loop, 32 bytes: odd part of k, its 2-adic
+// valuation, the offset of its character table (kNoTable if none), k, its first
+// row, the residues mod Q that have rows (bit r; Q <= 32), floor(2^64 / odd part).
+struct __align__(16) KInfo {
+  uint32_t k_odd, k_e2, k_jac, k_val, row0, rmask;
+  uint64_t k_rcp;
+};
+
 // Job constants, passed by value to every kernel (lives in the constant bank).
 struct JobDev {
   uint32_t base;
@@ -87,6 +95,7 @@ struct JobDev {
   const uint32_t *bitmap;    // [nrows * words_per_row], bit (x - x_lo) of row
   const uint32_t *jac_bits;  // quadratic-character tables: bit a of table k' = (a/k') == +1
   const uint32_t *k_jac;     // [nk] word offset of k's table, or kNoTable
+  const KInfo *kinfo;        // [nk] the same per-k data packed for the setup kernel
   uint32_t b_odd, b_e2;
   uint64_t b_rcp;
   uint32_t b_jac;

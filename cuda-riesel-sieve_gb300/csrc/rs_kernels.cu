@@ -213,8 +213,16 @@ __device__ __forceinline__ void flush_table_round(const SetupWarpSmem &S, uint64
 
 // One thread per prime (a warp per 32 consecutive primes).  Lanes past the
 // chunk's prime count compute on a stand-in prime and store nothing.
+constexpr uint32_t kSetupKStage = 256;  // per-k records staged in shared memory (8 KB)
+
 __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   __shared__ SetupWarpSmem smem[4];
+  __shared__ KInfo sk[kSetupKStage];
+  // the per-k records, read by every thread of the block in the row loop
+  const bool kstaged = J.nk <= kSetupKStage;
+  if (kstaged)
+    for (uint32_t c = threadIdx.x; c < J.nk; c += blockDim.x) sk[c] = J.kinfo[c];
+  __syncthreads();
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   SetupWarpSmem &S = smem[warp];
   const uint32_t i0 = blockIdx.x * blockDim.x + warp * 32;
@@ -310,58 +318,101 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const bool qeven = (J.Q & 1u) == 0;
   uint32_t nact = 0;
   uint64_t vprev = 0, rp0 = 0, rp1 = 0;
-#pragma unroll 1
-  for (uint32_t c0 = 0; c0 < J.nk; c0 += 4) {
-    // the four characters first, so their table loads are in flight together;
-    // kept as 2-bit fields (character + 1) so that no array goes to local memory
-    uint32_t chpack = 0;
-#pragma unroll
-    for (uint32_t u = 0; u < 4; u++) {
-      const uint32_t c = c0 + u;
-      const int ch = c < J.nk ? legendre_k_tab(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c], J.k_jac[c], J.jac_bits) : 0;
-      chpack |= (uint32_t)(ch + 1) << (2 * u);
+  // one active row: its start value V and its row id, packed into the record
+  auto emit = [&](uint64_t V, uint32_t row) {
+    if (nact & 1) {
+      if (live) rec_st2(rec, J.el_v + nact - 1, vprev, V);
+    } else {
+      vprev = V;
     }
+    const uint64_t rbits = (uint64_t)row << (16 * (nact & 3));
+    if (nact & 4) rp1 |= rbits;
+    else rp0 |= rbits;
+    if ((nact & 7) == 7) {
+      if (live) rec_st2(rec, J.el_row + (nact >> 2) - 1, rp0, rp1);
+      rp0 = rp1 = 0;
+    }
+    nact++;
+  };
+  if (regtab) {
+    // Q <= 8: the rows of k are its residues present (KInfo.rmask, r ascending),
+    // the active ones follow from the two characters, and V = k * HB[r]; all
+    // per-k data comes from one 32-byte record (shared memory when staged).
 #pragma unroll 1
-    for (uint32_t u = 0; u < 4; u++) {
-      const uint32_t c = c0 + u;
-      int chik = (int)((chpack >> (2 * u)) & 3u) - 1;
-      if (c >= J.nk) break;
-      if (J.sign > 0) chik *= chim1;  // character of -k
-      if (chik == 0) continue;        // p | k
-      const uint32_t r0 = J.k_row0[c], r1 = J.k_row0[c + 1];
-      const uint64_t kmod = p > J.k_val[c] ? (uint64_t)J.k_val[c] : (uint64_t)J.k_val[c] % p;
-      const uint64_t kx = J.sign > 0 ? p - kmod : kmod;  // -k for k*b^n+1
-      uint64_t V = 0;
-      uint32_t cur = 0;
-      bool have = false;
+    for (uint32_t c0 = 0; c0 < J.nk; c0 += 4) {
+      // the four characters first, so their table loads are in flight together;
+      // kept as 2-bit fields (character + 1) so that no array goes to local memory
+      uint32_t chpack = 0;
+#pragma unroll
+      for (uint32_t u = 0; u < 4; u++) {
+        const uint32_t c = c0 + u;
+        int ch = 0;
+        if (c < J.nk) {
+          const KInfo &ki = kstaged ? sk[c] : J.kinfo[c];
+          ch = legendre_k_tab(p, ki.k_odd, ki.k_e2, ki.k_rcp, ki.k_jac, J.jac_bits);
+        }
+        chpack |= (uint32_t)(ch + 1) << (2 * u);
+      }
 #pragma unroll 1
-      for (uint32_t row = r0; row < r1; row++) {
-        const uint32_t r = J.row_r[row];
-        const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
-        if (!act) continue;
-        if (regtab) {
-          V = shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p);
-        } else {
+      for (uint32_t u = 0; u < 4; u++) {
+        const uint32_t c = c0 + u;
+        int chik = (int)((chpack >> (2 * u)) & 3u) - 1;
+        if (c >= J.nk) break;
+        if (J.sign > 0) chik *= chim1;  // character of -k
+        if (chik == 0) continue;        // p | k
+        const KInfo ki = kstaged ? sk[c] : J.kinfo[c];
+        uint32_t amask;
+        if (qeven)  // even r: (k/p) = 1; odd r: (k/p)(b/p) = 1
+          amask = (chik == 1 ? ki.rmask & 0x55555555u : 0u) | (chik * chib == 1 ? ki.rmask & 0xaaaaaaaau : 0u);
+        else
+          amask = (chib == -1 || chik == 1) ? ki.rmask : 0u;
+        if (!amask) continue;
+        const uint64_t kmod = p > ki.k_val ? (uint64_t)ki.k_val : (uint64_t)ki.k_val % p;
+        const uint64_t kx = J.sign > 0 ? p - kmod : kmod;  // -k for k*b^n+1
+#pragma unroll 1
+        while (amask) {
+          const uint32_t r = __ffs(amask) - 1;
+          amask &= amask - 1;
+          emit(shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p), ki.row0 + __popc(ki.rmask & ((1u << r) - 1)));
+        }
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (uint32_t c0 = 0; c0 < J.nk; c0 += 4) {
+      uint32_t chpack = 0;
+#pragma unroll
+      for (uint32_t u = 0; u < 4; u++) {
+        const uint32_t c = c0 + u;
+        const int ch = c < J.nk ? legendre_k_tab(p, J.k_odd[c], J.k_e2[c], J.k_rcp[c], J.k_jac[c], J.jac_bits) : 0;
+        chpack |= (uint32_t)(ch + 1) << (2 * u);
+      }
+#pragma unroll 1
+      for (uint32_t u = 0; u < 4; u++) {
+        const uint32_t c = c0 + u;
+        int chik = (int)((chpack >> (2 * u)) & 3u) - 1;
+        if (c >= J.nk) break;
+        if (J.sign > 0) chik *= chim1;  // character of -k
+        if (chik == 0) continue;        // p | k
+        const uint32_t r0 = J.k_row0[c], r1 = J.k_row0[c + 1];
+        const uint64_t kmod = p > J.k_val[c] ? (uint64_t)J.k_val[c] : (uint64_t)J.k_val[c] % p;
+        const uint64_t kx = J.sign > 0 ? p - kmod : kmod;  // -k for k*b^n+1
+        uint64_t V = 0;
+        uint32_t cur = 0;
+        bool have = false;
+#pragma unroll 1
+        for (uint32_t row = r0; row < r1; row++) {
+          const uint32_t r = J.row_r[row];
+          const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
+          if (!act) continue;
           if (!have) {
             V = montmul(montmul(kx, r2, M), H, M);
             have = true;
           }
 #pragma unroll 1
           for (; cur < r; cur++) V = shoup_mul(V, bmod, bq, p);
+          emit(V, row);
         }
-        if (nact & 1) {
-          if (live) rec_st2(rec, J.el_v + nact - 1, vprev, V);
-        } else {
-          vprev = V;
-        }
-        const uint64_t rbits = (uint64_t)row << (16 * (nact & 3));
-        if (nact & 4) rp1 |= rbits;
-        else rp0 |= rbits;
-        if ((nact & 7) == 7) {
-          if (live) rec_st2(rec, J.el_row + (nact >> 2) - 1, rp0, rp1);
-          rp0 = rp1 = 0;
-        }
-        nact++;
       }
     }
   }
