@@ -85,9 +85,25 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
   long line = 0;
   uint64_t total = 0;
   while (i < len) {
+    line++;
+    if (text[i] >= '0' && text[i] <= '9' && !out.k.empty()) {
+      // the common line, a decimal n delta: digits, optional trailing blanks, newline
+      uint64_t d = 0;
+      size_t c = i;
+      while (c < len && c - i < 11 && (unsigned)(text[c] - '0') < 10u) d = d * 10 + (uint64_t)(text[c++] - '0');
+      size_t c2 = c;
+      while (c2 < len && (text[c2] == '\r' || text[c2] == ' ' || text[c2] == '\t')) c2++;
+      if (c - i <= 10 && (c2 == len || text[c2] == '\n')) {
+        if (d == 0) return fail(RS_ERR_INVALID, "ABCD line %ld: bad n delta", line);
+        total += d;
+        if (total > 0x7fffffffull) return fail(RS_ERR_INVALID, "ABCD line %ld: n exceeds 2^31-1", line);
+        out.n.back().push_back((uint32_t)total);
+        i = c2 + 1;
+        continue;
+      }
+    }
     size_t e = i;
     while (e < len && text[e] != '\n') e++;
-    line++;
     size_t a = i, z = e;
     i = e + 1;
     while (z > a && (text[z - 1] == '\r' || text[z - 1] == ' ' || text[z - 1] == '\t')) z--;
