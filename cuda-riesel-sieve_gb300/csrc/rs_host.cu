@@ -593,6 +593,11 @@ static int upload_job(rs_job *j) {
   d.Q = pl.Q;
   d.m = pl.m;
   d.cta_warps = pl.cta ? kCtaWarps : 1;
+  {
+    bool all_both = pl.Q == 2;
+    for (size_t i = 0; all_both && i < s.k.size(); i++) all_both = pl.k_row0[i + 1] - pl.k_row0[i] == 2;
+    d.pairable = all_both && d.cta_warps == 1 ? 1u : 0u;
+  }
   d.chain_len = (pl.m + 64 * d.cta_warps - 1) / (64 * d.cta_warps);
   {
     uint64_t bq = 1;

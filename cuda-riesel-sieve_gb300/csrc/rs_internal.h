@@ -31,7 +31,8 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // CTA-per-prime kernel): chain c covers j = c*chain_len + t, each step a
 // product by B = b^Q.  Thread t of the prime's group (t = 32*warp + lane) owns
 // chains t and t + 32W.  Element map:
-//   0 p, 1 pinv, 2 B, 3 G^32 (giant stride), 4 nact, 5 floor(2^64 / p),
+//   0 p, 1 pinv, 2 B, 3 G^32 (giant stride), 4 nact (low word; high word 1 if the
+//   active rows come in (k, 0), (k, 1) pairs, see pairable), 5 floor(2^64 / p),
 //   6,7 B in normal form and its Shoup constant (the chain step),
 //   8,9 B^(32W*chain_len) likewise (chain t -> chain t+32W), 10,11 G^32 likewise,
 //   W > 1 only: 12.. B^(32w*chain_len) for w < W likewise (pairs; warp w's offset),
@@ -64,6 +65,7 @@ struct JobDev {
   uint32_t cta_warps;    // warps per prime: 1 (bsgs_kernel) or kCtaWarps (bsgs_cta_kernel)
   uint32_t el_v;         // first element of V (kElV, or kElWoff + 2*cta_warps)
   uint32_t bq_small;     // b^Q as an integer when below 2^32, else 0
+  uint32_t pairable;     // Q == 2, a warp per prime and every k has rows for both residues
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes

@@ -422,7 +422,11 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBm, B, Gs);
   // floor(2^64/p) is the Shoup constant of 1, whose Montgomery form is `one`
-  rec_st2(rec, kElNact, pb ? 0 : nact, shoup_const(one, M.pinv));
+  // With (b/p) = 1 and both residues of every k present, k's two rows are both
+  // active or both not, so the active rows come in adjacent (k, 0), (k, 1) pairs
+  // whose start values differ by the factor b.
+  const uint64_t paired = (J.pairable && chib == 1) ? 1ull << 32 : 0ull;
+  rec_st2(rec, kElNact, pb ? 0 : (nact | paired), shoup_const(one, M.pinv));
   // the strides in normal form with their Shoup constants, once per prime
   rec_st2(rec, kElStw, from_mont(B, p, M.pinv), shoup_const(B, M.pinv));
   rec_st2(rec, kElGw, from_mont(Gs, p, M.pinv), shoup_const(Gs, M.pinv));
@@ -665,10 +669,12 @@ __device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList 
 // Giant steps with one step per row slot: lane (lane_row) multiplies the V of
 // slots gi*RPI + lane_row and (gi+1)*RPI + lane_row by its G^(lane_t+1) and
 // tests the home buckets; bit gi/2 of hA (hB) records a hit or full bucket.
-template <uint32_t RPI>
+// PAIRED (RPI == 1 only): slots gi, gi+1 hold a (k, 0), (k, 1) pair, so the
+// second value is the first times the integer b (the short product).
+template <uint32_t RPI, bool PAIRED = false>
 __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *__restrict__ Vs, uint32_t ngi,
                                            uint32_t nact, uint32_t lane_row, uint64_t Glw, uint64_t Glq, uint64_t p,
-                                           uint32_t &hA, uint32_t &hB) {
+                                           uint32_t &hA, uint32_t &hB, uint32_t b = 0, uint32_t rc = 0) {
 #pragma unroll 2
   for (uint32_t gi = 0; gi < ngi; gi += 2) {
     uint64_t va, vb;
@@ -685,7 +691,7 @@ __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *_
       vb = Vs[min(sa + RPI, nact - 1)];
     }
     const uint64_t ya = shoup_mul(va, Glw, Glq, p);
-    const uint64_t yb = shoup_mul(vb, Glw, Glq, p);
+    const uint64_t yb = PAIRED ? mul_small(ya, b, rc, p) : shoup_mul(vb, Glw, Glq, p);
     const uint32_t bit = 1u << (gi >> 1);
     if (W.probe_home(ya)) hA |= bit;
     if (W.probe_home(yb)) hB |= bit;
@@ -818,7 +824,11 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         // Separate calls for staged and global V keep each load's address
         // space known to the compiler.
         uint32_t hA = 0, hB = 0;
-        if (J.stage_full)
+        const bool paired = RPI == 1 && cb.small_step && (cur[kElNact] >> 32);
+        if (paired && J.stage_full)
+          giant_home<RPI, RPI == 1>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                    (uint32_t)cur[kElRcp]);
+        else if (J.stage_full)
           giant_home<RPI>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         else
           giant_home<RPI>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
