@@ -15,6 +15,18 @@ def _set(f):
     return [(int(a), int(b), int(c)) for a, b, c in f]
 
 
+_WIDE = []
+
+
+def _wide_job():
+    """The wide job (40M candidates, slow to generate), made once per session."""
+    import rsieve.synth as S
+
+    if not _WIDE:
+        _WIDE.append(S.wide_job(1))
+    return _WIDE[0]
+
+
 def _both(rs, oracle_mod, base, sign, ks, nlists, p0, p1, datless=False, **opts):
     job = rs.Job(base=base, sign=sign, ks=ks, nlists=nlists, datless=int(datless), **opts)
     g, st = job.sieve(p0, p1)
@@ -181,7 +193,7 @@ def test_wide_config_window(rs, oracle_mod):
     2e6-wide window at 2^50, complete and datless."""
     import rsieve.synth as S
 
-    b, s, ks, nl = S.wide_job(1)
+    b, s, ks, nl = _wide_job()
     p0 = S.WIDE_RANGE[0]
     for datless in (False, True):
         g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**6, datless=datless)
@@ -218,3 +230,19 @@ def test_autotune_keeps_results(rs):
     assert _set(got) == _set(want) and len(want) > 0
     assert info["Q"] >= 1 and info["baby_steps"] * info["giant_steps"] >= info["x_range"]
     assert info["num_candidates"] == before["num_candidates"]
+
+
+@pytest.mark.parametrize("hash_m,sign", [(11, -1), (12, 1)])
+def test_cta_layout_more_giant_steps(rs, oracle_mod, hash_m, sign):
+    """The CTA-per-prime kernel with 8 and 4 giant steps per lane (baby steps
+    capped by -m), both signs, against the oracle near 2^50."""
+    import rsieve.synth as S
+
+    b, _, ks, nl = _wide_job()
+    p0 = S.WIDE_RANGE[0]
+    job = rs.Job(base=b, sign=sign, ks=ks, nlists=nl, hash_m=hash_m)
+    assert job.info["warps_per_prime"] == 16 and job.info["giant_steps"] >= 128
+    job.close()
+    g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, p0, p0 + 5 * 10**5, hash_m=hash_m)
+    assert g == o
+    assert st["primes"] > 10000
