@@ -246,3 +246,15 @@ def test_cta_layout_more_giant_steps(rs, oracle_mod, hash_m, sign):
     g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, p0, p0 + 5 * 10**5, hash_m=hash_m)
     assert g == o
     assert st["primes"] > 10000
+
+
+def test_sierpinski_row_pairs_near_1e13(rs, oracle_mod):
+    """k*b^n+1 on the dense benchmark-shaped job at 1e13, where the baby steps
+    use the short product and primes with (b/p) = 1 take the row-pair path."""
+    import rsieve.synth as S
+
+    b, _, ks, nl = S.plain_job(3)
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, b, 1, ks, nl, 10**13, 10**13 + 2 * 10**7, datless=datless)
+        assert g == o
+    assert st["primes"] > 600000
