@@ -9,9 +9,9 @@
 namespace rs {
 
 // BSGS fast path: per-prime hash of 16-bit tags, kBucket tags per 16-byte bucket.
-constexpr uint32_t kEmptyTag = 0xffffu;
 constexpr int kBucket = 8;
-constexpr int kMatchCap = 15;       // deferred tag matches per prime before the exact path
+constexpr int kMatchCap = 15;       // deferred tag matches per prime before the exact path (15 keeps
+                                    // the benchmark job at five 4-warp CTAs per SM)
 // BSGS exact path (rare primes): 32-bit entries (tag << jbits) | j, linear probing.
 // j <= m-1 <= 2^jbits - 2, so a real entry is never all ones.
 constexpr uint32_t kEmpty = 0xffffffffu;
@@ -31,7 +31,7 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // CTA-per-prime kernel): chain c covers j = c*chain_len + t, each step a
 // product by B = b^Q.  Thread t of the prime's group (t = 32*warp + lane) owns
 // chains t and t + 32W.  Element map:
-//   0 p, 1 pinv, 2 B, 3 G^32 (giant stride), 4 nact (low word; high word 1 if the
+//   0 p, 1 pinv, 2 B, 3 G^32 (spare: the kernels use 10,11), 4 nact (low word; high word 1 if the
 //   active rows come in (k, 0), (k, 1) pairs, see pairable), 5 floor(2^64 / p),
 //   6,7 B in normal form and its Shoup constant (the chain step),
 //   8,9 B^(32W*chain_len) likewise (chain t -> chain t+32W), 10,11 G^32 likewise,
@@ -82,9 +82,9 @@ struct JobDev {
   uint32_t rec_elems;    // 64-bit elements per prime record
   uint32_t el_row;       // first element of the row-id array
   uint32_t el_tab;       // first element of the per-lane tables (B^lane, then G^(lane % tlanes + 1))
-  uint32_t stage_elems;  // elements of a record staged in shared memory (all, or the first kElV)
+  uint32_t stage_elems;  // elements staged per record by bsgs_kernel: header + V (el_row), or the header (el_v)
   uint32_t stage_full;   // 1 if V and row ids are read from the staged copy
-  uint32_t warp_smem;    // shared-memory bytes per warp in the fast BSGS kernel
+  uint32_t warp_smem;    // shared-memory bytes per warp (bsgs_kernel) or per CTA (bsgs_cta_kernel)
   uint32_t exact_log2;   // slots of the exact kernel's table = 1 << exact_log2
   // device arrays
   const uint32_t *row_r;     // [nrows] n mod Q of each row

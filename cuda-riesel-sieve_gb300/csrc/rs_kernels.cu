@@ -1,22 +1,30 @@
 // rs_kernels.cu -- the sieve's device kernels for sm_103a.
 //
-//   sieve_kernel   segmented Eratosthenes over odd numbers; one 2^18-odd
-//                  segment per CTA in shared memory; writes the primes of a
-//                  p-window straight into HBM.  Replaces the host prime
-//                  generator generateGPUPrimes (kernel_v0.24.6.cu:1838-1987),
-//                  but is complete (every composite removed) where the
-//                  reference leaves composites above smallP_max^2.
+//   sieve_large_kernel, sieve_small_kernel
+//                  segmented Eratosthenes over odd numbers: primes >= 65536
+//                  once per window into an L2-resident bitmap, smaller ones
+//                  per 2^15-odd segment in shared memory, then compaction; the
+//                  primes of a p-window go straight into HBM.  Replaces the
+//                  host prime generator generateGPUPrimes
+//                  (kernel_v0.24.6.cu:1838-1987), but is complete (every
+//                  composite removed) where the reference leaves composites
+//                  above smallP_max^2.
 //   setup_kernel   one thread per prime: Montgomery constants, B = b^Q, the
 //                  quadratic-character filter per (k, n mod Q) row
 //                  (kernel_v0.24.6.cu:461-521), the per-row giant-step start
 //                  values k*b^r*B^e0 (kernel_v0.24.6.cu:454-509,525-528) and the
-//                  per-lane power tables the BSGS kernel starts from.
-//   bsgs_kernel    one prime per warp: baby steps B^j (j < m) into a
-//                  shared-memory open-addressing table, then giant steps for
-//                  every active row, 32 lanes sharing each prime
-//                  (kernel_v0.24.6.cu:365-620 is the per-thread, global-memory
-//                  original).  Candidate hits are checked against the row
-//                  bitmap on the device and appended with one atomic each.
+//                  per-lane power tables the BSGS kernels start from.
+//   bsgs_kernel    one prime per warp: baby steps B^j (j < m) in 64 chains of
+//                  consecutive exponents into a shared-memory table of 16-bit
+//                  tags, then giant steps for every active row, 32 lanes per
+//                  prime (kernel_v0.24.6.cu:365-620 is the per-thread,
+//                  global-memory original).  Candidate hits are checked
+//                  against the row bitmap on the device and appended with one
+//                  atomic each.
+//   bsgs_cta_kernel  the same with a CTA of 16 warps per prime and one large
+//                  table, for jobs with many k or wide n ranges.
+//   bsgs_exact_kernel  the rare primes whose tag matches overflow the fast
+//                  path's list, with an exact (tag, j) table.
 //   verify_kernel  direct k*b^n check of every hit (kernel_v0.24.6.cu:1649-1671).
 #include <cstdio>
 
