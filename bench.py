@@ -286,9 +286,13 @@ def run_served(args) -> None:
         j.sieve(top[2] - 10**6, top[2])
     t0 = time.perf_counter()
     plain = []
+    t_create = gpu_plain = 0.0
     for abcd, p0, p1 in jobs:
+        tc = time.perf_counter()
         with rsieve.Job(abcd) as j:
-            f, _ = j.sieve(p0, p1)
+            t_create += time.perf_counter() - tc
+            f, st = j.sieve(p0, p1)
+        gpu_plain += st["gpu_ms"] / 1e3
         plain.append(key(f))
     t_plain = time.perf_counter() - t0
 
@@ -346,9 +350,10 @@ def run_served(args) -> None:
         "dtype": "u64", "data": "synthetic (seeded)",
         "config": {"workload": f"{n} jobs of rsieve.synth.batch_job(1, i), p-window {width} wide each",
                    "slots": args.slots, "mem_budget_gib": 64, "queue_cap": 1024},
-        "plain": {"p_per_s": total_width / t_plain, "wall_s": t_plain},
+        # create_s: host parse + plan + upload; gpu_s: summed device time of the sieve calls
+        "plain": {"p_per_s": total_width / t_plain, "wall_s": t_plain, "create_s": t_create, "gpu_s": gpu_plain},
         "batched": {"p_per_s": total_width / t_batch, "wall_s": t_batch, "vs_plain": t_plain / t_batch,
-                    "jobs_per_s": capacity},
+                    "jobs_per_s": capacity, "gpu_s": sum(r["gpu_ms"] for r in reps) / 1e3},
         "served": served,
         "results_match_plain": bool(ok_batch and ok_served),
     }
@@ -372,7 +377,7 @@ def main() -> None:
     ap.add_argument("--served-jobs", type=int, default=64)
     ap.add_argument("--served-window", type=float, default=1e8,
                     help="p-window width of each job (the batch shape's 1e9 makes a run of 64 jobs take ~10 min)")
-    ap.add_argument("--served-loads", type=float, nargs="*", default=[0.5, 1.0, 1.5])
+    ap.add_argument("--served-loads", type=float, nargs="*", default=[0.25, 0.5, 1.0, 1.5])
     ap.add_argument("--slots", type=int, default=4, help="jobs running at once in the served form")
     args = ap.parse_args()
     select_workload(args.workload)

@@ -518,7 +518,16 @@ static int upload_job(rs_job *j) {
     off = align_up(off + bytes, 256);
     return o;
   };
-  const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4);
+  // k*b^r per row; the job takes the integer-row layout when all are below 2^32
+  std::vector<uint32_t> row_c(pl.row_r.size(), 0);
+  bool int_rows = !row_c.empty();
+  for (size_t r = 0; r < row_c.size(); r++) {
+    uint64_t c = s.k[pl.row_kidx[r]];
+    for (uint32_t e = 0; e < pl.row_r[r] && c < (1ull << 32); e++) c *= s.base;
+    if (c >= (1ull << 32)) int_rows = false;
+    else row_c[r] = (uint32_t)c;
+  }
+  const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4), o_rc = sec(row_c.size() * 4);
   const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
   const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
   // Quadratic-character tables, one per distinct odd part > 1 of k and b,
@@ -556,6 +565,7 @@ static int upload_job(rs_job *j) {
   std::vector<uint8_t> host(o_jb, 0);
   memcpy(host.data() + o_rr, pl.row_r.data(), pl.row_r.size() * 4);
   memcpy(host.data() + o_rk, pl.row_kidx.data(), pl.row_kidx.size() * 4);
+  memcpy(host.data() + o_rc, row_c.data(), row_c.size() * 4);
   memcpy(host.data() + o_kv, s.k.data(), nk * 4);
   memcpy(host.data() + o_ko, kodd.data(), nk * 4);
   memcpy(host.data() + o_ke, ke2.data(), nk * 4);
@@ -638,6 +648,8 @@ static int upload_job(rs_job *j) {
     d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
+  d.row_c = (const uint32_t *)(b + o_rc);
+  d.int_rows = int_rows ? 1u : 0u;
   d.k_val = (const uint32_t *)(b + o_kv);
   d.k_odd = (const uint32_t *)(b + o_ko);
   d.k_e2 = (const uint32_t *)(b + o_ke);

@@ -40,6 +40,15 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 //   4 per element), el_tab.. B^(lane*chain_len) (32 elements, the chain starts
 //   of warp 0), el_tab+32.. G^(lane % tlanes + 1) (32 elements).
 // Residues are in Montgomery form unless marked normal.
+//
+// Integer rows (JobDev::int_rows, every row's k*b^r below 2^32): the giant value
+// of row (k, r) at step s is c*Z_s with the integer c = k*b^r and
+// Z_s = +-B^e0 * G^s (the sign of k*b^n+-1 folded in).  Then V[] holds the
+// integers c, and el_tab+32.. holds Z_(lane % tlanes + 1) times 2^128 mod p
+// instead of G^(lane % tlanes + 1) times 2^64: the kernels' normal-form
+// multiplier from_mont(entry) is then Z's Montgomery form, so Shoup's product
+// c*from_mont(entry), and equally montmul(c, entry), is the Montgomery form of
+// the giant value, as V*G^s is in the general layout.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kElRcp = 5;
 constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
 constexpr uint32_t kElWoff = 12;   // warp offsets (W > 1)
@@ -66,6 +75,7 @@ struct JobDev {
   uint32_t el_v;         // first element of V (kElV, or kElWoff + 2*cta_warps)
   uint32_t bq_small;     // b^Q as an integer when below 2^32, else 0
   uint32_t pairable;     // Q == 2, a warp per prime and every k has rows for both residues
+  uint32_t int_rows;     // every row's k*b^r < 2^32: V holds these integers (see the record layout)
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes
@@ -89,6 +99,7 @@ struct JobDev {
   // device arrays
   const uint32_t *row_r;     // [nrows] n mod Q of each row
   const uint32_t *row_kidx;  // [nrows] index of the row's k
+  const uint32_t *row_c;     // [nrows] k*b^r (meaningful when int_rows)
   const uint32_t *k_val;     // [nk]
   const uint32_t *k_odd;     // [nk] odd part of k
   const uint32_t *k_e2;      // [nk] 2-adic valuation of k

@@ -278,7 +278,14 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
     // value t of the G table is G^(t % tlanes + 1): the chain restarts at G
     // whenever t % tlanes wraps to 0 (tlanes divides 32)
     const uint64_t Gw = from_mont(G, p, M.pinv), Gq = shoup_const(G, M.pinv);
-    uint64_t g = G;
+    // integer rows: the table holds Z_(t+1) = +-B^e0 * G^(t+1) times 2^128 instead
+    uint64_t g0 = G;
+    if (J.int_rows) {
+      uint64_t h2 = montmul(H, r2, M);  // B^e0 times 2^128
+      if (J.sign > 0 && h2) h2 = p - h2;
+      g0 = shoup_mul(h2, Gw, Gq, p);
+    }
+    uint64_t g = g0;
     uint32_t k = 0;
 #pragma unroll 1
     for (uint32_t h = 0; h < 2; h++) {
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           pair[u] = g;
           if (++k == J.tlanes) {
             k = 0;
-            g = G;
+            g = g0;
           } else {
             g = shoup_mul(g, Gw, Gq, p);
           }
@@ -301,15 +308,22 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
       }
       flush_table_round(S, cb.recs, J.rec_elems, i0, n, J.el_tab + 32 + 16 * h, lane);
     }
-    if (J.tlanes != 32) Gs = 0;
+    if (J.tlanes != 32) {
+      Gs = 0;
+    } else if (J.int_rows) {  // the table's last entry is Z_32: G^32 by squaring
+      Gs = G;
+#pragma unroll 1
+      for (uint32_t q = 0; q < 5; q++) Gs = montmul(Gs, Gs, M);
+    }
   }
 
   // HB[r] = b^r * B^e0 (Montgomery form) with the Shoup constant of HB[r] taken
-  // as an integer, so the start value of row (k, r) is the single product k*HB[r].
+  // as an integer, so the start value of row (k, r) is the single product k*HB[r]
+  // (not needed for integer rows).
   // Kept per thread in shared memory (indexed by r without a select chain); the
   // staging area is free again after the last flush.
   const bool regtab = J.Q <= kSetupRegQ;
-  if (regtab) {
+  if (regtab && !J.int_rows) {
     uint64_t h = H;
 #pragma unroll 1
     for (uint32_t r = 0; r < J.Q; r++) {
@@ -319,8 +333,9 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
     }
   }
 
-  // Active rows (quadratic-character filter) and their giant-step start values,
-  // written in pairs (V) and in groups of eight (row ids) as 16-byte stores.
+  // Active rows (quadratic-character filter) and their giant-step start values
+  // (the integers k*b^r for integer rows), written in pairs (V) and in groups of
+  // eight (row ids) as 16-byte stores.
   const int chib = legendre_k_tab(p, J.b_odd, J.b_e2, J.b_rcp, J.b_jac, J.jac_bits);
   const int chim1 = ((uint32_t)p & 3u) == 1u ? 1 : -1;  // (-1/p)
   const bool qeven = (J.Q & 1u) == 0;
@@ -381,7 +396,9 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
         while (amask) {
           const uint32_t r = __ffs(amask) - 1;
           amask &= amask - 1;
-          emit(shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p), ki.row0 + __popc(ki.rmask & ((1u << r) - 1)));
+          const uint32_t row = ki.row0 + __popc(ki.rmask & ((1u << r) - 1));
+          emit(J.int_rows ? (uint64_t)__ldg(J.row_c + row) : shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p),
+               row);
         }
       }
     }
@@ -413,6 +430,10 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           const uint32_t r = J.row_r[row];
           const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
           if (!act) continue;
+          if (J.int_rows) {
+            emit(__ldg(J.row_c + row), row);
+            continue;
+          }
           if (!have) {
             V = montmul(montmul(kx, r2, M), H, M);
             have = true;
@@ -679,7 +700,9 @@ __device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList 
 // tests the home buckets; bit gi/2 of hA (hB) records a hit or full bucket.
 // PAIRED (RPI == 1 only): slots gi, gi+1 hold a (k, 0), (k, 1) pair, so the
 // second value is the first times the integer b (the short product).
-template <uint32_t RPI, bool PAIRED = false>
+// INT: integer rows, V holds k*b^r < 2^32 and Glw the lane's Z (Shoup's
+// product with a 32-bit operand).
+template <uint32_t RPI, bool PAIRED = false, bool INT = false>
 __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *__restrict__ Vs, uint32_t ngi,
                                            uint32_t nact, uint32_t lane_row, uint64_t Glw, uint64_t Glq, uint64_t p,
                                            uint32_t &hA, uint32_t &hB, uint32_t b = 0, uint32_t rc = 0) {
@@ -698,8 +721,9 @@ __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *_
       va = Vs[min(sa, nact - 1)];
       vb = Vs[min(sa + RPI, nact - 1)];
     }
-    const uint64_t ya = shoup_mul(va, Glw, Glq, p);
-    const uint64_t yb = PAIRED ? mul_small(ya, b, rc, p) : shoup_mul(vb, Glw, Glq, p);
+    const uint64_t ya = INT ? shoup_mul32((uint32_t)va, Glw, Glq, p) : shoup_mul(va, Glw, Glq, p);
+    const uint64_t yb = PAIRED ? mul_small(ya, b, rc, p)
+                               : (INT ? shoup_mul32((uint32_t)vb, Glw, Glq, p) : shoup_mul(vb, Glw, Glq, p));
     const uint32_t bit = 1u << (gi >> 1);
     if (W.probe_home(ya)) hA |= bit;
     if (W.probe_home(yb)) hB |= bit;
@@ -714,8 +738,9 @@ __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *_
 // Each lane runs two independent product chains in both phases (baby steps
 // j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
 // time) so that consecutive dependent Shoup products overlap.
-// TL = giant steps handled side by side per row (min(T, 32)).
-template <int TL>
+// TL = giant steps handled side by side per row (min(T, 32)); INT = integer
+// rows (JobDev::int_rows).
+template <int TL, bool INT>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
@@ -834,12 +859,12 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         uint32_t hA = 0, hB = 0;
         const bool paired = RPI == 1 && cb.small_step && (cur[kElNact] >> 32);
         if (paired && J.stage_full)
-          giant_home<RPI, RPI == 1>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
-                                    (uint32_t)cur[kElRcp]);
+          giant_home<RPI, RPI == 1, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                         (uint32_t)cur[kElRcp]);
         else if (J.stage_full)
-          giant_home<RPI>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+          giant_home<RPI, false, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         else
-          giant_home<RPI>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+          giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         if (hA | hB) {
 #pragma unroll 1
           for (uint32_t h = 0; h < 2; h++) {
@@ -860,8 +885,9 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         for (uint32_t gi = 0; gi < ngi; gi += 2) {
           const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
           const bool aa = sa < nact, ab = sb < nact;
-          uint64_t ya = shoup_mul(Vs[min(sa, nact - 1)], Glw, Glq, p);
-          uint64_t yb = shoup_mul(Vs[min(sb, nact - 1)], Glw, Glq, p);
+          const uint64_t va = Vs[min(sa, nact - 1)], vb = Vs[min(sb, nact - 1)];
+          uint64_t ya = INT ? shoup_mul32((uint32_t)va, Glw, Glq, p) : shoup_mul(va, Glw, Glq, p);
+          uint64_t yb = INT ? shoup_mul32((uint32_t)vb, Glw, Glq, p) : shoup_mul(vb, Glw, Glq, p);
           uint32_t s = lane_t + 1;
 #pragma unroll 1
           for (uint32_t u = 0;; u++) {
@@ -914,19 +940,83 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 
 typedef void (*BsgsFn)(JobDev, ChunkBufs, HitBufs);
 
-static BsgsFn bsgs_fn(uint32_t tlanes) {
+template <bool INT>
+static BsgsFn bsgs_fn_t(uint32_t tlanes) {
   switch (tlanes) {
-    case 1: return bsgs_kernel<1>;
-    case 2: return bsgs_kernel<2>;
-    case 4: return bsgs_kernel<4>;
-    case 8: return bsgs_kernel<8>;
-    case 16: return bsgs_kernel<16>;
-    default: return bsgs_kernel<32>;
+    case 1: return bsgs_kernel<1, INT>;
+    case 2: return bsgs_kernel<2, INT>;
+    case 4: return bsgs_kernel<4, INT>;
+    case 8: return bsgs_kernel<8, INT>;
+    case 16: return bsgs_kernel<16, INT>;
+    default: return bsgs_kernel<32, INT>;
   }
+}
+
+static BsgsFn bsgs_fn(const JobDev &job) {
+  return job.int_rows ? bsgs_fn_t<true>(job.tlanes) : bsgs_fn_t<false>(job.tlanes);
 }
 
 int bsgs_smem_bytes(const JobDev &job) {
   return job.cta_warps > 1 ? (int)job.warp_smem : kWarpsPerBlock * (int)job.warp_smem;
+}
+
+// Giant steps of the CTA kernel: warp w takes row slots w, w + W, ..., four at
+// a time (four independent product chains per lane).  The loop tests home
+// buckets only and records the outcome as bits (step u of slot k -> bit 4u + k,
+// spl <= 8); tag hits and full buckets are finished after each pass.  INT:
+// integer rows (V holds k*b^r < 2^32).  TWO (integer rows, spl == 2): the
+// second value of a slot is also c times a lane multiplier, Z advanced by G^32
+// (Glw2, Glq2), so both products are independent short ones.
+template <bool INT, bool TWO>
+__device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &ML, const uint64_t *vst, uint32_t nact,
+                                           uint32_t warp, uint32_t lane, uint32_t spl, uint64_t Glw, uint64_t Glq,
+                                           uint64_t Gw, uint64_t Gq, uint64_t p, uint64_t Glw2 = 0,
+                                           uint64_t Glq2 = 0) {
+#pragma unroll 1
+  for (uint32_t s0 = warp; s0 < nact; s0 += 4 * kCtaWarps) {
+    uint64_t y[4];
+    uint32_t c[4];
+    uint32_t valid = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < 4; k++) {
+      const uint32_t sl = s0 + k * kCtaWarps;
+      valid |= (sl < nact ? 0x11111111u : 0u) << k;
+      const uint64_t v = vst[sl < nact ? sl : s0];
+      c[k] = (uint32_t)v;
+      y[k] = INT ? shoup_mul32((uint32_t)v, Glw, Glq, p) : shoup_mul(v, Glw, Glq, p);
+    }
+    uint32_t bits = 0;
+    if (TWO) {
+      uint64_t z[4];
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++) z[k] = shoup_mul32(c[k], Glw2, Glq2, p);
+#pragma unroll
+      for (uint32_t k = 0; k < 4; k++) {
+        if (W.probe_home(y[k])) bits |= 1u << k;
+        if (W.probe_home(z[k])) bits |= 1u << (4 + k);
+      }
+    } else {
+#pragma unroll 1
+      for (uint32_t u = 0;; u++) {
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++)
+          if (W.probe_home(y[k])) bits |= 1u << (4 * u + k);
+        if (u + 1 >= spl) break;
+#pragma unroll
+        for (uint32_t k = 0; k < 4; k++) y[k] = shoup_mul(y[k], Gw, Gq, p);
+      }
+    }
+    bits &= valid;
+    while (bits) {  // rare
+      const uint32_t b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const uint32_t k = b & 3, u = b >> 2, sl = s0 + k * kCtaWarps;
+      uint64_t v = shoup_mul(vst[sl], Glw, Glq, p);
+#pragma unroll 1
+      for (uint32_t q = 0; q < u; q++) v = shoup_mul(v, Gw, Gq, p);
+      if (W.probe(v)) ML.push(v, sl, lane + 1 + 32 * u);
+    }
+  }
 }
 
 // The CTA-per-prime kernel, for jobs whose best baby-step count needs a table
@@ -939,6 +1029,7 @@ int bsgs_smem_bytes(const JobDev &job) {
 // V is staged with cp.async during the baby steps.  Table operations, the
 // deferred overflow inserts and the exact tag-match resolution are those of
 // bsgs_kernel; hits are pushed where they are found (tag matches are rare).
+template <bool INT>
 __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
   constexpr uint32_t G = 32 * kCtaWarps;
@@ -1009,43 +1100,20 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
       __syncthreads();
     }
 
-    // Giant steps: warp w takes row slots w, w + W, ..., four at a time (four
-    // independent product chains per lane).  The loop tests home buckets only
-    // and records the outcome as bits (step u of slot k -> bit 4u + k, spl <= 8);
-    // tag hits and full buckets are finished after each pass.
+    // Giant steps (cta_giants)
     const uint64_t Glm = rec[J.el_tab + 32 + lane];
     const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
     const uint64_t Gw = rec[kElGw], Gq = rec[kElGq];
-#pragma unroll 1
-    for (uint32_t s0 = warp; s0 < nact; s0 += 4 * kCtaWarps) {
-      uint64_t y[4];
-      uint32_t valid = 0;
-#pragma unroll
-      for (uint32_t k = 0; k < 4; k++) {
-        const uint32_t sl = s0 + k * kCtaWarps;
-        valid |= (sl < nact ? 0x11111111u : 0u) << k;
-        y[k] = shoup_mul(vst[sl < nact ? sl : s0], Glw, Glq, p);
+    if constexpr (INT) {
+      if (spl == 2) {
+        const uint64_t E2 = shoup_mul(Glm, Gw, Gq, p);  // Z advanced by G^32, times 2^128
+        cta_giants<true, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, from_mont(E2, p, pinv),
+                               shoup_const(E2, pinv));
+      } else {
+        cta_giants<true, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p);
       }
-      uint32_t bits = 0;
-#pragma unroll 1
-      for (uint32_t u = 0;; u++) {
-#pragma unroll
-        for (uint32_t k = 0; k < 4; k++)
-          if (W.probe_home(y[k])) bits |= 1u << (4 * u + k);
-        if (u + 1 >= spl) break;
-#pragma unroll
-        for (uint32_t k = 0; k < 4; k++) y[k] = shoup_mul(y[k], Gw, Gq, p);
-      }
-      bits &= valid;
-      while (bits) {  // rare
-        const uint32_t b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const uint32_t k = b & 3, u = b >> 2, sl = s0 + k * kCtaWarps;
-        uint64_t v = shoup_mul(vst[sl], Glw, Glq, p);
-#pragma unroll 1
-        for (uint32_t q = 0; q < u; q++) v = shoup_mul(v, Gw, Gq, p);
-        if (W.probe(v)) ML.push(v, sl, lane + 1 + 32 * u);
-      }
+    } else {
+      cta_giants<false, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p);
     }
     __syncthreads();
 
@@ -1198,7 +1266,8 @@ static cudaError_t configure_one(const void *fn, int smem, int threads, int devi
 static int bsgs_threads(const JobDev &job) { return job.cta_warps > 1 ? 32 * kCtaWarps : 32 * kWarpsPerBlock; }
 
 static const void *bsgs_fast_fn(const JobDev &job) {
-  return job.cta_warps > 1 ? (const void *)bsgs_cta_kernel : (const void *)bsgs_fn(job.tlanes);
+  if (job.cta_warps > 1) return job.int_rows ? (const void *)bsgs_cta_kernel<true> : (const void *)bsgs_cta_kernel<false>;
+  return (const void *)bsgs_fn(job);
 }
 
 static const void *bsgs_exact_fn(const JobDev &job) {
@@ -1214,9 +1283,10 @@ cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *ex
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st) {
   if (job.cta_warps > 1)
-    bsgs_cta_kernel<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+    (job.int_rows ? bsgs_cta_kernel<true> : bsgs_cta_kernel<false>)<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(
+        job, cb, hb);
   else
-    bsgs_fn(job.tlanes)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+    bsgs_fn(job)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();
 }
 
