@@ -68,6 +68,19 @@ __device__ __forceinline__ uint64_t shoup_mul32(uint32_t c, uint64_t w, uint64_t
   return (int64_t)s < 0 ? r : s;
 }
 
+// Shoup's product by a small fixed multiplier: x*w mod p for w < 2^32 with
+// w * 2^32 < p, so that wq = floor(w * 2^64 / p) < 2^32.  The quotient
+// estimate floor(x * wq / 2^64) < wq then needs two 32x32 multiply-adds, and
+// the bound is Shoup's (any x < 2^64, r in [0, 2p)).
+__device__ __forceinline__ uint64_t shoup_mul_w32(uint64_t x, uint32_t w, uint32_t wq, uint64_t p) {
+  const uint64_t t = (uint64_t)(uint32_t)x * wq;
+  const uint64_t u = (x >> 32) * (uint64_t)wq + (t >> 32);
+  const uint32_t q = (uint32_t)(u >> 32);
+  const uint64_t r = x * (uint64_t)w + (uint64_t)q * (0 - p);
+  const uint64_t s = r - p;
+  return (int64_t)s < 0 ? r : s;
+}
+
 // x*c mod p for a small integer multiplier c, with rc = floor(2^64 / p).
 // Requires x < p, 2^33 < p and c*p < 2^63.  Then P = x*c < 2^63 and the
 // quotient estimate q' = floor(hi32(P) * rc / 2^32) satisfies

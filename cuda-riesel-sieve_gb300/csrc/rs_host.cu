@@ -1037,10 +1037,15 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
         e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
       {
-        // short baby-step products need p > 2^33 and b^Q * p < 2^63 for every p of the chunk
+        // short baby-step products need p > 2^33 and b^Q * p < 2^63 for every p
+        // of the chunk; Shoup's product with a 32-bit constant needs b^Q * 2^32 < p
         const uint64_t bq = j->dev.bq_small;
-        j->cb.small_step = bq != 0 && todo[c].a > (1ull << 33) &&
-                           (unsigned __int128)bq * todo[c].b < ((unsigned __int128)1 << 63);
+        if (bq != 0 && todo[c].a > (1ull << 33) && (unsigned __int128)bq * todo[c].b < ((unsigned __int128)1 << 63))
+          j->cb.small_step = kStepSmall;
+        else if (bq != 0 && (bq << 32) < todo[c].a)
+          j->cb.small_step = kStepHigh;
+        else
+          j->cb.small_step = kStepShoup;
       }
       if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
       if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);

@@ -53,6 +53,7 @@ constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kEl
 constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
 constexpr uint32_t kElWoff = 12;   // warp offsets (W > 1)
 constexpr uint32_t kElV = 12;      // V in the warp-per-prime layout (W == 1)
+constexpr uint32_t kStepShoup = 0, kStepSmall = 1, kStepHigh = 2;  // ChunkBufs::small_step
 constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
 constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
@@ -128,8 +129,10 @@ struct ChunkBufs {
   uint32_t *redo;       // [cap] primes handed to the exact BSGS kernel
   uint32_t *redo_count; // [1]
   uint32_t cap;
-  // 1 if every prime p of the chunk has p > 2^33 and b^Q * p < 2^63, so that a
-  // baby step is the short product by the small integer b^Q (mul_small)
+  // The baby step of the chunk: kStepSmall if every prime p of the chunk has
+  // p > 2^33 and b^Q * p < 2^63 (the short product by the integer b^Q,
+  // mul_small), kStepHigh if b^Q < 2^32 and b^Q * 2^32 < p (Shoup's product
+  // with a 32-bit constant), else kStepShoup (Shoup's product).
   uint32_t small_step;
 };
 

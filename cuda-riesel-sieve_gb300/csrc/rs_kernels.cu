@@ -675,6 +675,12 @@ struct StepSmall {
   uint64_t p;
   __device__ __forceinline__ uint64_t operator()(uint64_t x) const { return mul_small(x, c, rc, p); }
 };
+// b^Q * 2^32 < p (large primes): Shoup's product with a 32-bit constant.
+struct StepHigh {
+  uint32_t w, wq;
+  uint64_t p;
+  __device__ __forceinline__ uint64_t operator()(uint64_t x) const { return shoup_mul_w32(x, w, wq, p); }
+};
 
 // Baby steps of one lane: two chains of `len` steps from va and vb, of which
 // the first na (nb) are inserted (all of them when FULL).  A value whose home bucket is full is
@@ -818,12 +824,14 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       // until the giant steps) and are inserted after the loop.
       uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
       if (J.m == 64 * CL) {  // every chain full (the planner's usual choice of m)
-        if (cb.small_step)
+        // (kStepHigh chunks take Shoup's product here: a third baby loop in this
+        // kernel measured slower on the short-product path)
+        if (cb.small_step == kStepSmall)
           baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
         else
           baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
       } else {
-        if (cb.small_step)
+        if (cb.small_step == kStepSmall)
           baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
         else
           baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
@@ -857,7 +865,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         // Separate calls for staged and global V keep each load's address
         // space known to the compiler.
         uint32_t hA = 0, hB = 0;
-        const bool paired = RPI == 1 && cb.small_step && (cur[kElNact] >> 32);
+        const bool paired = RPI == 1 && cb.small_step == kStepSmall && (cur[kElNact] >> 32);
         if (paired && J.stage_full)
           giant_home<RPI, RPI == 1, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
                                          (uint32_t)cur[kElRcp]);
@@ -1078,8 +1086,10 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
     uint64_t Bl = rec[J.el_tab + lane];
     if (warp) Bl = shoup_mul(Bl, rec[kElWoff + 2 * warp], rec[kElWoff + 2 * warp + 1], p);
     const uint64_t Blb = shoup_mul(Bl, rec[kElOfw], rec[kElOfq], p);
-    if (cb.small_step)
+    if (cb.small_step == kStepSmall)
       baby_chains<true>(W, ML, ovf, Bl, Blb, CL, CL, CL, StepSmall{J.bq_small, (uint32_t)rec[kElRcp], p});
+    else if (cb.small_step == kStepHigh)
+      baby_chains<true>(W, ML, ovf, Bl, Blb, CL, CL, CL, StepHigh{J.bq_small, (uint32_t)rec[kElStq], p});
     else
       baby_chains<true>(W, ML, ovf, Bl, Blb, CL, CL, CL, StepShoup{rec[kElStw], rec[kElStq], p});
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -1128,7 +1138,7 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
       uint64_t va = Bl, vb = Blb;
       const uint64_t Stw = rec[kElStw], Stq = rec[kElStq];
       const uint32_t bq = J.bq_small, rcp = (uint32_t)rec[kElRcp];
-      const bool small = cb.small_step != 0;
+      const bool small = cb.small_step == kStepSmall;
 #pragma unroll 1
       for (uint32_t t = 0; t < CL; t++) {
 #pragma unroll 1
