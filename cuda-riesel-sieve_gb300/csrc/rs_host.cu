@@ -495,6 +495,29 @@ static void pinned_put(void *p, size_t bytes) {
   g_pin_free.push_back({p, align_up(bytes, 4096)});
 }
 
+// Form of the giant-step start values (rs_job_info.row_form): kRowsV (V in
+// Montgomery form per active row), kRowsIntV (the integers k*b^r, all below
+// 2^32, in V) or kRowsIntId (no V: the kernels read k*b^r by row id).  The last
+// when the warp kernel could not stage header + V whole anyway, or when the CTA
+// kernel takes two or more giant steps per lane from each start value: there
+// the lookup costs less than the setup kernel's V stores (measured on mixed
+// jobs).  row_c receives k*b^r per row.
+static uint32_t plan_row_form(const Plan &pl, const Seqs &s, std::vector<uint32_t> *row_c) {
+  if (row_c) row_c->assign(pl.row_r.size(), 0);
+  bool ints = !pl.row_r.empty();
+  for (size_t r = 0; r < pl.row_r.size() && ints; r++) {
+    uint64_t c = s.k[pl.row_kidx[r]];
+    for (uint32_t e = 0; e < pl.row_r[r] && c < (1ull << 32); e++) c *= s.base;
+    if (c >= (1ull << 32)) ints = false;
+    else if (row_c) (*row_c)[r] = (uint32_t)c;
+  }
+  if (!ints) return kRowsV;
+  const uint32_t vslots = (std::max<uint32_t>(1, pl.nrows) + 1) & ~1u;
+  const uint32_t el_v = pl.cta ? kElWoff + 2 * kCtaWarps : kElV;
+  const bool ids = pl.cta ? pl.steps_per_lane >= 2 : (el_v + vslots) * 8 > 2048;
+  return ids ? kRowsIntId : kRowsIntV;
+}
+
 static int upload_job(rs_job *j) {
   const Plan &pl = j->plan;
   const Seqs &s = j->seqs;
@@ -518,15 +541,8 @@ static int upload_job(rs_job *j) {
     off = align_up(off + bytes, 256);
     return o;
   };
-  // k*b^r per row; the job takes the integer-row layout when all are below 2^32
-  std::vector<uint32_t> row_c(pl.row_r.size(), 0);
-  bool int_rows = !row_c.empty();
-  for (size_t r = 0; r < row_c.size(); r++) {
-    uint64_t c = s.k[pl.row_kidx[r]];
-    for (uint32_t e = 0; e < pl.row_r[r] && c < (1ull << 32); e++) c *= s.base;
-    if (c >= (1ull << 32)) int_rows = false;
-    else row_c[r] = (uint32_t)c;
-  }
+  std::vector<uint32_t> row_c;
+  const uint32_t form = plan_row_form(pl, s, &row_c);
   const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4), o_rc = sec(row_c.size() * 4);
   const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
   const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
@@ -631,13 +647,18 @@ static int upload_job(rs_job *j) {
   d.words_per_row = pl.words_per_row;
   d.datless = j->opt.datless ? 1u : 0u;
   d.max_act = std::max<uint32_t>(1, pl.nrows);
+  d.int_rows = form != kRowsV ? 1u : 0u;
+  d.row_ids_only = form == kRowsIntId ? 1u : 0u;  // no V in the record
   d.el_v = d.cta_warps > 1 ? kElWoff + 2 * d.cta_warps : kElV;
-  d.el_row = d.el_v + ((d.max_act + 1) & ~1u);  // even: row ids are written 16 bytes at a time
+  d.el_row = d.el_v + (d.row_ids_only ? 0u : ((d.max_act + 1) & ~1u));  // even: row ids are written 16 bytes at a time
   d.el_tab = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
   d.rec_elems = d.el_tab + 64;
-  if (d.el_row * 8 <= 2048) {
+  // the warp kernel's staged part of a record: header + V (header + row ids
+  // without V) when it fits 2 KB; else the header alone
+  const uint32_t staged = d.row_ids_only ? d.el_tab : d.el_row;
+  if (staged * 8 <= 2048) {
     d.stage_full = 1;
-    d.stage_elems = d.el_row;
+    d.stage_elems = staged;
   } else {
     d.stage_full = 0;
     d.stage_elems = d.el_v;
@@ -649,7 +670,6 @@ static int upload_job(rs_job *j) {
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.row_c = (const uint32_t *)(b + o_rc);
-  d.int_rows = int_rows ? 1u : 0u;
   d.k_val = (const uint32_t *)(b + o_kv);
   d.k_odd = (const uint32_t *)(b + o_ko);
   d.k_e2 = (const uint32_t *)(b + o_ke);
@@ -924,6 +944,7 @@ int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   info->work_per_prime = pl.work_per_prime;
   info->upload_bytes = j->job_bytes;
   info->warps_per_prime = pl.cta ? kCtaWarps : 1;
+  info->row_form = plan_row_form(pl, j->seqs, nullptr);
   return RS_OK;
 }
 
@@ -1290,6 +1311,7 @@ extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp
   info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
   info->work_per_prime = pl.work_per_prime;
   info->warps_per_prime = pl.cta ? kCtaWarps : 1;
+  info->row_form = plan_row_form(pl, s, nullptr);
   return RS_OK;
 }
 

@@ -48,12 +48,18 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // instead of G^(lane % tlanes + 1) times 2^64: the kernels' normal-form
 // multiplier from_mont(entry) is then Z's Montgomery form, so Shoup's product
 // c*from_mont(entry), and equally montmul(c, entry), is the Montgomery form of
-// the giant value, as V*G^s is in the general layout.
+// the giant value, as V*G^s is in the general layout.  With row_ids_only the
+// record has no V at all (el_row == el_v) and the kernels read c from row_c by
+// the row id; this halves the setup kernel's scattered stores for jobs whose V
+// would not be staged whole anyway.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kElRcp = 5;
 constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
 constexpr uint32_t kElWoff = 12;   // warp offsets (W > 1)
 constexpr uint32_t kElV = 12;      // V in the warp-per-prime layout (W == 1)
 constexpr uint32_t kStepShoup = 0, kStepSmall = 1, kStepHigh = 2;  // ChunkBufs::small_step
+// Giant-step start values of the fast kernels (template argument): V in
+// Montgomery form, the integers k*b^r in V, or k*b^r read by row id.
+constexpr int kRowsV = 0, kRowsIntV = 1, kRowsIntId = 2;
 constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
 constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
@@ -77,6 +83,7 @@ struct JobDev {
   uint32_t bq_small;     // b^Q as an integer when below 2^32, else 0
   uint32_t pairable;     // Q == 2, a warp per prime and every k has rows for both residues
   uint32_t int_rows;     // every row's k*b^r < 2^32: V holds these integers (see the record layout)
+  uint32_t row_ids_only; // integer rows whose records keep no V: the kernels read k*b^r by row id
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes

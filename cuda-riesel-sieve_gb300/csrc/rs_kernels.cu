@@ -342,9 +342,10 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   uint32_t nact = 0;
   uint64_t vprev = 0, rp0 = 0, rp1 = 0;
   // one active row: its start value V and its row id, packed into the record
+  // (integer rows: the row id only, the kernels look up k*b^r by it)
   auto emit = [&](uint64_t V, uint32_t row) {
     if (nact & 1) {
-      if (live) rec_st2(rec, J.el_v + nact - 1, vprev, V);
+      if (live && !J.row_ids_only) rec_st2(rec, J.el_v + nact - 1, vprev, V);
     } else {
       vprev = V;
     }
@@ -397,7 +398,8 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           const uint32_t r = __ffs(amask) - 1;
           amask &= amask - 1;
           const uint32_t row = ki.row0 + __popc(ki.rmask & ((1u << r) - 1));
-          emit(J.int_rows ? (uint64_t)__ldg(J.row_c + row) : shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p),
+          emit(J.int_rows ? (J.row_ids_only ? 0 : (uint64_t)__ldg(J.row_c + row))
+                          : shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p),
                row);
         }
       }
@@ -431,7 +433,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
           if (!act) continue;
           if (J.int_rows) {
-            emit(__ldg(J.row_c + row), row);
+            emit(J.row_ids_only ? 0 : (uint64_t)__ldg(J.row_c + row), row);
             continue;
           }
           if (!have) {
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
     }
   }
   if (!live) return;
-  if (nact & 1) rec[J.el_v + nact - 1] = vprev;
+  if ((nact & 1) && !J.row_ids_only) rec[J.el_v + nact - 1] = vprev;
   if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBm, B, Gs);
@@ -706,8 +708,7 @@ __device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList 
 // tests the home buckets; bit gi/2 of hA (hB) records a hit or full bucket.
 // PAIRED (RPI == 1 only): slots gi, gi+1 hold a (k, 0), (k, 1) pair, so the
 // second value is the first times the integer b (the short product).
-// INT: integer rows, V holds k*b^r < 2^32 and Glw the lane's Z (Shoup's
-// product with a 32-bit operand).
+// INT: integer rows with k*b^r in V (Shoup's product for a 32-bit operand).
 template <uint32_t RPI, bool PAIRED = false, bool INT = false>
 __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *__restrict__ Vs, uint32_t ngi,
                                            uint32_t nact, uint32_t lane_row, uint64_t Glw, uint64_t Glq, uint64_t p,
@@ -736,6 +737,35 @@ __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *_
   }
 }
 
+// The same for integer rows: slot gi holds a row id (16 bits), whose k*b^r is
+// read from the job's table (read-only cache) and multiplied by the lane's Z
+// with Shoup's product for a 32-bit operand.  A slot past nact (RPI == 1, nact
+// odd) repeats slot gi; its outcome is discarded after the loop.
+template <uint32_t RPI, bool PAIRED = false>
+__device__ __forceinline__ void giant_home_int(const WarpTable &W, const uint16_t *__restrict__ Rs,
+                                               const uint32_t *__restrict__ ctab, uint32_t ngi, uint32_t nact,
+                                               uint32_t lane_row, uint64_t Glw, uint64_t Glq, uint64_t p, uint32_t &hA,
+                                               uint32_t &hB, uint32_t b = 0, uint32_t rc = 0) {
+#pragma unroll 2
+  for (uint32_t gi = 0; gi < ngi; gi += 2) {
+    uint32_t ra, rb;
+    if (RPI == 1) {
+      const uint32_t rr = *reinterpret_cast<const uint32_t *>(Rs + gi);  // slots gi, gi+1 (gi even)
+      ra = rr & 0xffffu;
+      rb = gi + 1 < nact ? rr >> 16 : ra;
+    } else {
+      const uint32_t sa = gi * RPI + lane_row;
+      ra = Rs[min(sa, nact - 1)];
+      rb = Rs[min(sa + RPI, nact - 1)];
+    }
+    const uint64_t ya = shoup_mul32(__ldg(ctab + ra), Glw, Glq, p);
+    const uint64_t yb = PAIRED ? mul_small(ya, b, rc, p) : shoup_mul32(__ldg(ctab + rb), Glw, Glq, p);
+    const uint32_t bit = 1u << (gi >> 1);
+    if (W.probe_home(ya)) hA |= bit;
+    if (W.probe_home(yb)) hB |= bit;
+  }
+}
+
 // Per-warp shared memory of the fast kernel:
 //   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
 // The stages hold a record's header and V (double-buffered with cp.async); each
@@ -744,9 +774,9 @@ __device__ __forceinline__ void giant_home(const WarpTable &W, const uint64_t *_
 // Each lane runs two independent product chains in both phases (baby steps
 // j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
 // time) so that consecutive dependent Shoup products overlap.
-// TL = giant steps handled side by side per row (min(T, 32)); INT = integer
-// rows (JobDev::int_rows).
-template <int TL, bool INT>
+// TL = giant steps handled side by side per row (min(T, 32)); RM = the form
+// of the giant-step start values (kRowsV, kRowsIntV, kRowsIntId).
+template <int TL, int RM>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
@@ -858,6 +888,15 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
       const uint32_t ngi = (nact + RPI - 1) / RPI;
       const uint64_t *Vs = J.stage_full ? cur + kElV : cb.recs + (size_t)i * J.rec_elems + kElV;
+      // integer rows: the row ids (16 bits) of the staged or global record
+      const uint16_t *Rs = reinterpret_cast<const uint16_t *>(
+          J.stage_full ? cur + J.el_row : cb.recs + (size_t)i * J.rec_elems + J.el_row);
+      // the giant value of slot sl (the general and the integer-row form)
+      auto giant_val = [&](uint32_t sl) -> uint64_t {
+        if constexpr (RM == kRowsIntId) return shoup_mul32(__ldg(J.row_c + Rs[sl]), Glw, Glq, p);
+        else if constexpr (RM == kRowsIntV) return shoup_mul32((uint32_t)Vs[sl], Glw, Glq, p);
+        else return shoup_mul(Vs[sl], Glw, Glq, p);
+      };
       if (spl == 1 && ngi <= 64) {
         // One giant step per slot.  The loop only tests each value's home
         // bucket and collects the outcome as bits (pass gi of chain A or B ->
@@ -866,13 +905,25 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         // space known to the compiler.
         uint32_t hA = 0, hB = 0;
         const bool paired = RPI == 1 && cb.small_step == kStepSmall && (cur[kElNact] >> 32);
-        if (paired && J.stage_full)
-          giant_home<RPI, RPI == 1, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
-                                         (uint32_t)cur[kElRcp]);
-        else if (J.stage_full)
-          giant_home<RPI, false, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
-        else
-          giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+        if constexpr (RM == kRowsIntId) {
+          const uint16_t *Rst = reinterpret_cast<const uint16_t *>(cur + J.el_row);
+          if (paired && J.stage_full)
+            giant_home_int<RPI, RPI == 1>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                          (uint32_t)cur[kElRcp]);
+          else if (J.stage_full)
+            giant_home_int<RPI>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+          else
+            giant_home_int<RPI>(W, Rs, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+        } else {
+          constexpr bool INT = RM == kRowsIntV;
+          if (paired && J.stage_full)
+            giant_home<RPI, RPI == 1, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                           (uint32_t)cur[kElRcp]);
+          else if (J.stage_full)
+            giant_home<RPI, false, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+          else
+            giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+        }
         if (hA | hB) {
 #pragma unroll 1
           for (uint32_t h = 0; h < 2; h++) {
@@ -882,7 +933,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
               bits &= bits - 1;
               const uint32_t sl = g * RPI + lane_row;
               if (sl < nact) {
-                const uint64_t y = shoup_mul(Vs[sl], Glw, Glq, p);
+                const uint64_t y = giant_val(sl);
                 if (W.probe(y)) ML.push(y, sl, lane_t + 1);
               }
             }
@@ -893,9 +944,8 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         for (uint32_t gi = 0; gi < ngi; gi += 2) {
           const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
           const bool aa = sa < nact, ab = sb < nact;
-          const uint64_t va = Vs[min(sa, nact - 1)], vb = Vs[min(sb, nact - 1)];
-          uint64_t ya = INT ? shoup_mul32((uint32_t)va, Glw, Glq, p) : shoup_mul(va, Glw, Glq, p);
-          uint64_t yb = INT ? shoup_mul32((uint32_t)vb, Glw, Glq, p) : shoup_mul(vb, Glw, Glq, p);
+          uint64_t ya = giant_val(min(sa, nact - 1));
+          uint64_t yb = giant_val(min(sb, nact - 1));
           uint32_t s = lane_t + 1;
 #pragma unroll 1
           for (uint32_t u = 0;; u++) {
@@ -948,21 +998,30 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 
 typedef void (*BsgsFn)(JobDev, ChunkBufs, HitBufs);
 
-template <bool INT>
+template <int RM>
 static BsgsFn bsgs_fn_t(uint32_t tlanes) {
   switch (tlanes) {
-    case 1: return bsgs_kernel<1, INT>;
-    case 2: return bsgs_kernel<2, INT>;
-    case 4: return bsgs_kernel<4, INT>;
-    case 8: return bsgs_kernel<8, INT>;
-    case 16: return bsgs_kernel<16, INT>;
-    default: return bsgs_kernel<32, INT>;
+    case 1: return bsgs_kernel<1, RM>;
+    case 2: return bsgs_kernel<2, RM>;
+    case 4: return bsgs_kernel<4, RM>;
+    case 8: return bsgs_kernel<8, RM>;
+    case 16: return bsgs_kernel<16, RM>;
+    default: return bsgs_kernel<32, RM>;
   }
 }
 
-static BsgsFn bsgs_fn(const JobDev &job) {
-  return job.int_rows ? bsgs_fn_t<true>(job.tlanes) : bsgs_fn_t<false>(job.tlanes);
+static int row_mode(const JobDev &job) {
+  return job.row_ids_only ? kRowsIntId : job.int_rows ? kRowsIntV : kRowsV;
 }
+
+static BsgsFn bsgs_fn(const JobDev &job) {
+  switch (row_mode(job)) {
+    case kRowsIntId: return bsgs_fn_t<kRowsIntId>(job.tlanes);
+    case kRowsIntV: return bsgs_fn_t<kRowsIntV>(job.tlanes);
+    default: return bsgs_fn_t<kRowsV>(job.tlanes);
+  }
+}
+
 
 int bsgs_smem_bytes(const JobDev &job) {
   return job.cta_warps > 1 ? (int)job.warp_smem : kWarpsPerBlock * (int)job.warp_smem;
@@ -971,15 +1030,17 @@ int bsgs_smem_bytes(const JobDev &job) {
 // Giant steps of the CTA kernel: warp w takes row slots w, w + W, ..., four at
 // a time (four independent product chains per lane).  The loop tests home
 // buckets only and records the outcome as bits (step u of slot k -> bit 4u + k,
-// spl <= 8); tag hits and full buckets are finished after each pass.  INT:
-// integer rows (V holds k*b^r < 2^32).  TWO (integer rows, spl == 2): the
+// spl <= 8); tag hits and full buckets are finished after each pass.  RM: vst
+// holds V (kRowsV), the integers k*b^r (kRowsIntV) or 16-bit row ids whose
+// k*b^r come from the job's table ctab (kRowsIntId).  TWO (integer rows, spl == 2): the
 // second value of a slot is also c times a lane multiplier, Z advanced by G^32
 // (Glw2, Glq2), so both products are independent short ones.
-template <bool INT, bool TWO>
+template <int RM, bool TWO>
 __device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &ML, const uint64_t *vst, uint32_t nact,
                                            uint32_t warp, uint32_t lane, uint32_t spl, uint64_t Glw, uint64_t Glq,
-                                           uint64_t Gw, uint64_t Gq, uint64_t p, uint64_t Glw2 = 0,
-                                           uint64_t Glq2 = 0) {
+                                           uint64_t Gw, uint64_t Gq, uint64_t p, const uint32_t *__restrict__ ctab,
+                                           uint64_t Glw2 = 0, uint64_t Glq2 = 0) {
+  const uint16_t *rid = reinterpret_cast<const uint16_t *>(vst);
 #pragma unroll 1
   for (uint32_t s0 = warp; s0 < nact; s0 += 4 * kCtaWarps) {
     uint64_t y[4];
@@ -989,9 +1050,15 @@ __device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &
     for (uint32_t k = 0; k < 4; k++) {
       const uint32_t sl = s0 + k * kCtaWarps;
       valid |= (sl < nact ? 0x11111111u : 0u) << k;
-      const uint64_t v = vst[sl < nact ? sl : s0];
-      c[k] = (uint32_t)v;
-      y[k] = INT ? shoup_mul32((uint32_t)v, Glw, Glq, p) : shoup_mul(v, Glw, Glq, p);
+      if (RM == kRowsIntId) {
+        c[k] = __ldg(ctab + rid[sl < nact ? sl : s0]);
+        y[k] = shoup_mul32(c[k], Glw, Glq, p);
+      } else if (RM == kRowsIntV) {
+        c[k] = (uint32_t)vst[sl < nact ? sl : s0];
+        y[k] = shoup_mul32(c[k], Glw, Glq, p);
+      } else {
+        y[k] = shoup_mul(vst[sl < nact ? sl : s0], Glw, Glq, p);
+      }
     }
     uint32_t bits = 0;
     if (TWO) {
@@ -1019,7 +1086,9 @@ __device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &
       const uint32_t b = __ffs(bits) - 1;
       bits &= bits - 1;
       const uint32_t k = b & 3, u = b >> 2, sl = s0 + k * kCtaWarps;
-      uint64_t v = shoup_mul(vst[sl], Glw, Glq, p);
+      uint64_t v = RM == kRowsIntId  ? shoup_mul32(__ldg(ctab + rid[sl]), Glw, Glq, p)
+                   : RM == kRowsIntV ? shoup_mul32((uint32_t)vst[sl], Glw, Glq, p)
+                                     : shoup_mul(vst[sl], Glw, Glq, p);
 #pragma unroll 1
       for (uint32_t q = 0; q < u; q++) v = shoup_mul(v, Gw, Gq, p);
       if (W.probe(v)) ML.push(v, sl, lane + 1 + 32 * u);
@@ -1037,7 +1106,7 @@ __device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &
 // V is staged with cp.async during the baby steps.  Table operations, the
 // deferred overflow inserts and the exact tag-match resolution are those of
 // bsgs_kernel; hits are pushed where they are found (tag matches are rare).
-template <bool INT>
+template <int RM>
 __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
   constexpr uint32_t G = 32 * kCtaWarps;
@@ -1069,11 +1138,14 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
     if (nact == 0) continue;
     const uint64_t p = rec[kElP], pinv = rec[kElPinv];
     __syncthreads();  // the previous prime is done with the table, V and the list
-    // V of the active rows into shared memory, 16 bytes per copy
-    const uint32_t vn = (nact + 1) & ~1u;
+    // V of the active rows (integer rows: their 16-bit row ids) into shared
+    // memory, 16 bytes per copy
+    constexpr bool IDS = RM == kRowsIntId;
+    const uint32_t vn = IDS ? 2 * ((nact + 7) / 8) : (nact + 1) & ~1u;
+    const uint64_t *vsrc = rec + (IDS ? J.el_row : J.el_v);
 #pragma unroll 1
     for (uint32_t e = 2 * tid; e < vn; e += 2 * G)
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(vdst + 8 * e), "l"(rec + J.el_v + e)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(vdst + 8 * e), "l"(vsrc + e)
                    : "memory");
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     const uint4 z4 = make_uint4(0, 0, 0, 0);
@@ -1114,16 +1186,16 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
     const uint64_t Glm = rec[J.el_tab + 32 + lane];
     const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
     const uint64_t Gw = rec[kElGw], Gq = rec[kElGq];
-    if constexpr (INT) {
+    if constexpr (RM != kRowsV) {
       if (spl == 2) {
         const uint64_t E2 = shoup_mul(Glm, Gw, Gq, p);  // Z advanced by G^32, times 2^128
-        cta_giants<true, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, from_mont(E2, p, pinv),
-                               shoup_const(E2, pinv));
+        cta_giants<RM, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c,
+                               from_mont(E2, p, pinv), shoup_const(E2, pinv));
       } else {
-        cta_giants<true, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p);
+        cta_giants<RM, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
       }
     } else {
-      cta_giants<false, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p);
+      cta_giants<kRowsV, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
     }
     __syncthreads();
 
@@ -1223,7 +1295,9 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       const uint32_t slot = gi * rows_pass + wig * J.rows_per_it + lane_row;
       if (slot < nact) {
         const uint32_t row = (uint32_t)(rec_el(J, cb, J.el_row + (slot >> 2), i) >> (16 * (slot & 3))) & 0xffffu;
-        uint64_t y = montmul(rec_el(J, cb, J.el_v + slot, i), Gl, p, pinv);
+        // integer rows: montmul(k*b^r, Z * 2^128) is the Montgomery form of the giant value
+        uint64_t y =
+            montmul(J.row_ids_only ? (uint64_t)__ldg(J.row_c + row) : rec_el(J, cb, J.el_v + slot, i), Gl, p, pinv);
         uint32_t s = lane_t + 1;
 #pragma unroll 1
         for (uint32_t u = 0; u < J.steps_per_lane; u++) {
@@ -1275,8 +1349,16 @@ static cudaError_t configure_one(const void *fn, int smem, int threads, int devi
 
 static int bsgs_threads(const JobDev &job) { return job.cta_warps > 1 ? 32 * kCtaWarps : 32 * kWarpsPerBlock; }
 
+static BsgsFn bsgs_cta_fn(const JobDev &job) {
+  switch (row_mode(job)) {
+    case kRowsIntId: return bsgs_cta_kernel<kRowsIntId>;
+    case kRowsIntV: return bsgs_cta_kernel<kRowsIntV>;
+    default: return bsgs_cta_kernel<kRowsV>;
+  }
+}
+
 static const void *bsgs_fast_fn(const JobDev &job) {
-  if (job.cta_warps > 1) return job.int_rows ? (const void *)bsgs_cta_kernel<true> : (const void *)bsgs_cta_kernel<false>;
+  if (job.cta_warps > 1) return (const void *)bsgs_cta_fn(job);
   return (const void *)bsgs_fn(job);
 }
 
@@ -1293,8 +1375,7 @@ cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *ex
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
                         cudaStream_t st) {
   if (job.cta_warps > 1)
-    (job.int_rows ? bsgs_cta_kernel<true> : bsgs_cta_kernel<false>)<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(
-        job, cb, hb);
+    bsgs_cta_fn(job)<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   else
     bsgs_fn(job)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   return cudaGetLastError();

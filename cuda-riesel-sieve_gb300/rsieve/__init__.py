@@ -75,7 +75,7 @@ class JobInfo(ctypes.Structure):
         ("work_per_prime", ctypes.c_double),
         ("upload_bytes", ctypes.c_uint64),
         ("warps_per_prime", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("row_form", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

@@ -88,7 +88,8 @@ typedef struct {
   double work_per_prime; /* algorithmic montmuls per prime: 2*sqrt(E[R]*X) */
   uint64_t upload_bytes; /* host->device bytes copied when the job was created */
   uint32_t warps_per_prime; /* 1: a warp per prime; 16: a CTA per prime (large tables) */
-  uint32_t reserved;
+  uint32_t row_form;     /* giant-step start values: 0 per-prime residues, 1 the integers
+                            k*b^r (all < 2^32) in the records, 2 k*b^r read by row id */
 } rs_job_info;
 
 /* Counters and device-timed durations of the last rs_sieve_range call. */

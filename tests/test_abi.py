@@ -144,3 +144,19 @@ def test_plan_layouts(rs):
     # expected false tag matches per prime stay well inside the CTA match list
     er = d["rows"] * (0.5 if d["Q"] % 2 == 0 else 0.75)
     assert er * d["giant_steps"] * d["baby_steps"] / (d["table_slots"] / 8) / 65536 <= 16
+
+
+def test_plan_row_forms(rs, sr745_text):
+    """Giant-step start values: integers k*b^r in the records for the plain job
+    (k*745 < 2^32, a staged record), read by row id for the wide job (two giant
+    steps per lane on the CTA kernel), per-prime residues for sr_745.abcd
+    (Q = 18, so b^r is far above 2^32)."""
+    import rsieve.synth as S
+
+    assert rs.plan_abcd(S.to_abcd(*S.plain_job(1)))["row_form"] == 1
+    body = "\n".join(["1"] * 47 + [str(3 * 10**6 - 10**6 - 47)])
+    wide = "".join(f"ABCD {k}*2^$a-1 [1000000]\n{body}\n" for k in range(3, 2003, 2))
+    d = rs.plan_abcd(wide)
+    assert d["row_form"] == 2 and d["giant_steps"] >= 64
+    d = rs.plan_abcd(sr745_text)
+    assert d["Q"] > 2 and d["row_form"] == 0

@@ -214,6 +214,24 @@ def test_batch_shaped_jobs(rs, oracle_mod, i):
     assert g == o and st["primes"] > 1000
 
 
+@pytest.mark.parametrize("i,form,wpp", [(20, 1, 16), (5, 0, 16), (8, 2, 16), (4, 1, 1), (19, 1, 1), (62, 2, 1)])
+def test_row_forms(rs, oracle_mod, i, form, wpp):
+    """Each form of the giant-step start values on each kernel: per-prime
+    residues (form 0), the integers k*b^r kept in the records (form 1) and
+    k*b^r read by row id (form 2), with a warp (wpp 1) or a CTA (16) per
+    prime, on mixed-batch jobs at small p (with factors) and in their own
+    window near 2^60."""
+    import rsieve.synth as S
+
+    (b, s, ks, nl), (p0, _) = S.batch_job(7, i)
+    info = rs.plan_abcd(S.to_abcd(b, s, ks, nl), datless=1)
+    assert (info["row_form"], info["warps_per_prime"]) == (form, wpp)
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**6, 10**6 + 2 * 10**5, datless=True)
+    assert g == o and len(o) > 0
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**5, datless=True)
+    assert g == o and st["primes"] > 1000
+
+
 def test_autotune_keeps_results(rs):
     """Measured autotuning picks one of the cost model's cheapest layouts and
     leaves the factor set unchanged."""
