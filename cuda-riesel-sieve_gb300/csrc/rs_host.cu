@@ -851,14 +851,15 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out,
     return rc;
   }
   // primes per launch: -b/-t as in the reference (128*2^(b-1) blocks of
-  // 128*2^(t-1) threads, one prime each), else a memory budget of ~2 GB.
+  // 128*2^(t-1) threads, one prime each), else a memory budget of 3 GiB
+  // (larger launches measured 0.6% faster on the benchmark job than 2 GiB).
   uint64_t cap;
   if (opt.block_scale > 0 || opt.thread_scale > 0) {
     const int bs = opt.block_scale > 0 ? opt.block_scale : 1, ts = opt.thread_scale > 0 ? opt.thread_scale : 1;
     cap = (uint64_t)128 << (bs - 1);
     cap *= (uint64_t)128 << (ts - 1);
   } else {
-    const uint64_t budget = opt.mem_limit ? opt.mem_limit : (2ull << 30);
+    const uint64_t budget = opt.mem_limit ? opt.mem_limit : (3ull << 30);
     cap = budget / chunk_bytes_per_prime(j);
   }
   cap = std::max<uint64_t>(cap, 4096);

@@ -68,7 +68,7 @@ typedef struct {
   int32_t device;       /* CUDA device ordinal (the reference hard-codes 0) */
   int32_t reserved;     /* 0 */
   uint64_t mem_limit;   /* device bytes for the job's per-launch buffers, which set the
-                           primes per launch when -b/-t are not given; 0 = 2 GiB */
+                           primes per launch when -b/-t are not given; 0 = 3 GiB */
 } rs_options;
 
 /* The plan a job runs with. */
