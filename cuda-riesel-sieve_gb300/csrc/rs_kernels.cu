@@ -13,7 +13,9 @@
 //                  quadratic-character filter per (k, n mod Q) row
 //                  (kernel_v0.24.6.cu:461-521), the per-row giant-step start
 //                  values k*b^r*B^e0 (kernel_v0.24.6.cu:454-509,525-528) and the
-//                  per-lane power tables the BSGS kernels start from.
+//                  per-lane power tables the BSGS kernels start from.  For
+//                  integer rows (every k*b^r < 2^32) B^e0 moves into the lane
+//                  table and a start value is the integer k*b^r itself.
 //   bsgs_kernel    one prime per warp: baby steps B^j (j < m) in 64 chains of
 //                  consecutive exponents into a shared-memory table of 16-bit
 //                  tags, then giant steps for every active row, 32 lanes per
@@ -22,7 +24,9 @@
 //                  against the row bitmap on the device and appended with one
 //                  atomic each.
 //   bsgs_cta_kernel  the same with a CTA of 16 warps per prime and one large
-//                  table, for jobs with many k or wide n ranges.
+//                  table, for jobs with many k or wide n ranges.  Both are
+//                  instantiated per form of the start values (RM: per-prime
+//                  residues, integers in the record, integers by row id).
 //   bsgs_exact_kernel  the rare primes whose tag matches overflow the fast
 //                  path's list, with an exact (tag, j) table.
 //   verify_kernel  direct k*b^n check of every hit (kernel_v0.24.6.cu:1649-1671).
