@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rs_internal.h"
@@ -80,12 +81,53 @@ struct Seqs {
   std::vector<std::vector<uint32_t>> n;
 };
 
-static int parse_abcd(const char *text, size_t len, Seqs &out) {
+// One n-delta line "d..d\n" of 1 to 7 digits, read eight bytes at a time: the
+// digit count from the first non-digit byte (a byte b is a digit iff b - '0'
+// neither borrows nor exceeds 9), the value by Lemire's three-multiply decimal
+// conversion with the digits right-aligned among eight (leading zeros).
+// Borrows and carries only move towards later bytes, so every byte up to the
+// first non-digit is exact.  Needs 8 readable bytes at p and a little-endian
+// host.  Returns false for anything else (the general path handles it).
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "the 8-byte delta reader assumes little-endian loads");
+static inline bool delta8(const char *p, uint32_t &val, uint32_t &ndig) {
+  uint64_t w;
+  memcpy(&w, p, 8);
+  const uint64_t t = w - 0x3030303030303030ull;
+  const uint64_t nd = (t | (t + 0x7676767676767676ull)) & 0x8080808080808080ull;
+  if (!nd) return false;  // eight digits: longer than this reader takes
+  const uint32_t L = (uint32_t)__builtin_ctzll(nd) >> 3;
+  if (L == 0 || ((w >> (8 * L)) & 0xffu) != '\n') return false;
+  uint64_t d = t << (8 * (8 - L));  // the digits in the top L bytes, zeros below
+  d = d * 10 + (d >> 8);            // digit pairs
+  d = ((d & 0x000000FF000000FFull) * (100 + (1000000ull << 32)) +
+       ((d >> 16) & 0x000000FF000000FFull) * (1 + (10000ull << 32))) >> 32;
+  val = (uint32_t)d;
+  ndig = L;
+  return true;
+}
+
+static int parse_abcd_serial(const char *text, size_t len, Seqs &out) {
   size_t i = 0;
   long line = 0;
   uint64_t total = 0;
   while (i < len) {
     line++;
+    if (!out.k.empty() && i + 8 <= len) {
+      // runs of short delta lines, the bulk of a file
+      std::vector<uint32_t> &v = out.n.back();
+      uint32_t d, L;
+      bool first = true;
+      while (i + 8 <= len && delta8(text + i, d, L)) {
+        if (!first) line++;
+        first = false;
+        if (d == 0) return fail(RS_ERR_INVALID, "ABCD line %ld: bad n delta", line);
+        total += d;
+        if (total > 0x7fffffffull) return fail(RS_ERR_INVALID, "ABCD line %ld: n exceeds 2^31-1", line);
+        v.push_back((uint32_t)total);
+        i += L + 1;
+      }
+      if (!first) continue;
+    }
     if (text[i] >= '0' && text[i] <= '9' && !out.k.empty()) {
       // the common line, a decimal n delta: digits, optional trailing blanks, newline
       uint64_t d = 0;
@@ -169,6 +211,64 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
     }
   }
   if (out.k.empty()) return fail(RS_ERR_INVALID, "no ABCD header found");
+  return RS_OK;
+}
+
+// Large files are parsed in pieces on the host's cores: the text is cut at
+// "ABCD" header lines into contiguous ranges of about equal size, each range is
+// read by the serial reader into its own sequence list, and the lists are
+// concatenated in order.  Any error (or a base or sign that differs between
+// ranges) re-runs the serial reader on the whole text, so messages and line
+// numbers are those of the serial reader.
+static int parse_abcd(const char *text, size_t len, Seqs &out) {
+  constexpr size_t kPieceBytes = 4u << 20;
+  unsigned nthr = std::thread::hardware_concurrency();
+  if (nthr > 16) nthr = 16;
+  if (len < 2 * kPieceBytes || nthr < 2) return parse_abcd_serial(text, len, out);
+  if (len / kPieceBytes < nthr) nthr = (unsigned)(len / kPieceBytes);
+  // cut points: the first header line at or after len*t/nthr
+  std::vector<size_t> cut{0};
+  for (unsigned t = 1; t < nthr; t++) {
+    size_t q = std::max(cut.back() + 1, len * t / nthr);
+    bool found = false;
+    while (q + 5 < len) {
+      const void *nl = memchr(text + q, '\n', len - q);
+      if (!nl) break;
+      q = (size_t)((const char *)nl - text) + 1;
+      if (q + 4 <= len && memcmp(text + q, "ABCD", 4) == 0) {
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+    cut.push_back(q);
+  }
+  cut.push_back(len);
+  const size_t np = cut.size() - 1;
+  if (np < 2) return parse_abcd_serial(text, len, out);
+  std::vector<Seqs> part(np);
+  std::vector<int> rc(np, RS_OK);
+  std::vector<std::thread> th;
+  for (size_t t = 0; t < np; t++)
+    th.emplace_back([&, t] { rc[t] = parse_abcd_serial(text + cut[t], cut[t + 1] - cut[t], part[t]); });
+  for (auto &x : th) x.join();
+  bool ok = true;
+  for (size_t t = 0; t < np; t++)
+    ok = ok && rc[t] == RS_OK && part[t].base == part[0].base && part[t].sign == part[0].sign;
+  if (!ok) {
+    out = Seqs();
+    return parse_abcd_serial(text, len, out);
+  }
+  out.base = part[0].base;
+  out.sign = part[0].sign;
+  size_t nk = 0;
+  for (auto &p : part) nk += p.k.size();
+  out.k.reserve(nk);
+  out.n.reserve(nk);
+  for (auto &p : part) {
+    out.k.insert(out.k.end(), p.k.begin(), p.k.end());
+    for (auto &v : p.n) out.n.push_back(std::move(v));
+  }
   return RS_OK;
 }
 
@@ -376,41 +476,77 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
   pl.jbits = 1;
   while (((uint64_t)1 << pl.jbits) < (uint64_t)pl.m + 1) pl.jbits++;
   pl.words_per_row = (pl.X + 31) / 32;
-  // rows: k in input order, r ascending
+  // rows: k in input order, r ascending (the residues present: scan until all
+  // Q have been seen)
   const uint32_t Q = pl.Q;
-  pl.k_row0.assign(s.k.size() + 1, 0);
-  std::vector<int> rid(Q);
-  for (size_t i = 0; i < s.k.size(); i++) {
+  const size_t nk = s.k.size();
+  pl.k_row0.assign(nk + 1, 0);
+  std::vector<char> seen(Q);
+  for (size_t i = 0; i < nk; i++) {
     pl.k_row0[i] = (uint32_t)pl.row_r.size();
-    std::fill(rid.begin(), rid.end(), -1);
     if (datless) {
-      for (uint32_t r = 0; r < Q; r++) rid[r] = 1;
+      std::fill(seen.begin(), seen.end(), 1);
     } else {
-      for (uint32_t n : s.n[i]) rid[n % Q] = 1;
+      std::fill(seen.begin(), seen.end(), 0);
+      uint32_t got = 0;
+      for (uint32_t n : s.n[i])
+        if (!seen[n % Q]) {
+          seen[n % Q] = 1;
+          if (++got == Q) break;
+        }
     }
     for (uint32_t r = 0; r < Q; r++)
-      if (rid[r] >= 0) {
-        rid[r] = (int)pl.row_r.size();
+      if (seen[r]) {
         pl.row_r.push_back(r);
         pl.row_kidx.push_back((uint32_t)i);
       }
-    if (!datless && with_bitmap) {
-      // candidate bitmap rows (bits for x - x_lo)
-      size_t base_words = pl.bitmap.size();
-      size_t nr = pl.row_r.size() - pl.k_row0[i];
-      pl.bitmap.resize(base_words + nr * pl.words_per_row, 0);
-      for (uint32_t n : s.n[i]) {
-        const uint32_t r = n % Q;
-        const uint32_t row_local = (uint32_t)rid[r] - pl.k_row0[i];
-        const uint32_t bit = n / Q - pl.x_lo;
-        pl.bitmap[base_words + (size_t)row_local * pl.words_per_row + bit / 32] |= 1u << (bit & 31);
-      }
-    }
   }
-  pl.k_row0[s.k.size()] = (uint32_t)pl.row_r.size();
+  pl.k_row0[nk] = (uint32_t)pl.row_r.size();
   pl.nrows = (uint32_t)pl.row_r.size();
   if (pl.nrows > 65535) return fail(RS_ERR_INVALID, "too many (k, n mod Q) rows (%u > 65535)", pl.nrows);
-  if (datless) pl.bitmap.assign(1, 0);
+  if (datless) {
+    pl.bitmap.assign(1, 0);
+  } else if (with_bitmap) {
+    // candidate bitmap rows (bit x - x_lo of row (k, n mod Q)); the k are
+    // independent, so large jobs fill them on several host threads
+    pl.bitmap.assign((size_t)pl.nrows * pl.words_per_row, 0);
+    auto fill = [&](size_t k0, size_t k1) {
+      std::vector<uint32_t> local(Q);
+      for (size_t i = k0; i < k1; i++) {
+        for (uint32_t row = pl.k_row0[i]; row < pl.k_row0[i + 1]; row++) local[pl.row_r[row]] = row;
+        uint32_t *bm = pl.bitmap.data();
+        const uint32_t wpr = pl.words_per_row, xlo = pl.x_lo;
+        if (Q == 1) {
+          uint32_t *rowp = bm + (size_t)pl.k_row0[i] * wpr;
+          for (uint32_t n : s.n[i]) rowp[(n - xlo) >> 5] |= 1u << ((n - xlo) & 31);
+        } else {
+          for (uint32_t n : s.n[i]) {
+            const uint32_t x = n / Q, r = n - x * Q, bit = x - xlo;
+            bm[(size_t)local[r] * wpr + (bit >> 5)] |= 1u << (bit & 31);
+          }
+        }
+      }
+    };
+    size_t ncand = 0;
+    for (auto &v : s.n) ncand += v.size();
+    unsigned nthr = std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    if (ncand < (2u << 20) || nk < 2 * nthr) nthr = 1;
+    if (nthr == 1) {
+      fill(0, nk);
+    } else {
+      // k ranges of about equal candidate counts
+      std::vector<std::thread> th;
+      size_t k0 = 0, acc = 0;
+      for (size_t i = 0; i < nk; i++) {
+        acc += s.n[i].size();
+        if (acc * nthr >= ncand * (th.size() + 1) || i + 1 == nk) {
+          th.emplace_back(fill, k0, i + 1);
+          k0 = i + 1;
+        }
+      }
+      for (auto &x : th) x.join();
+    }
+  }
   return RS_OK;
 }
 

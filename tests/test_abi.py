@@ -75,6 +75,95 @@ def test_plan_sierpinski_and_crlf(rs):
     assert info["sign"] == 1 and info["num_candidates"] == 3 and info["nmax"] == 15
 
 
+def _py_parse(text):
+    """Plain restatement of the ABCD reading: per-k sorted, de-duplicated n."""
+    seqs, cur, total = {}, None, 0
+    for raw in text.split("\n"):
+        ln = raw.strip(" \t\r")
+        if not ln:
+            continue
+        if ln.startswith("ABCD"):
+            k = int(ln[5:].split("*")[0])
+            n0 = int(ln.split("[")[1].split("]")[0])
+            cur, total = seqs.setdefault(k, set()), n0
+            cur.add(n0)
+        else:
+            total += int(ln)
+            cur.add(total)
+    return {k: sorted(v) for k, v in seqs.items()}
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_abcd_parse_fuzz(rs, seed):
+    """The reader (8-byte fast path for short delta lines, general path for the
+    rest) against a plain restatement: deltas of 1 to 10 digits with leading
+    zeros, CRLF endings, blanks, blank lines, header comments, repeated k, and
+    files that end with or without a newline (the fast path needs 8 readable
+    bytes)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    parts = []
+    for _ in range(int(rng.integers(1, 6))):
+        k = int(rng.choice([3, 5, 7, 9, 11]))
+        n = int(rng.integers(1, 1000))
+        parts.append(f"ABCD {k}*2^$a-1 [{n}]" + (" // comment" if rng.random() < 0.3 else ""))
+        for _ in range(int(rng.integers(0, 400))):
+            nd = int(rng.choice([1, 1, 2, 2, 3, 4, 5, 6, 7, 8, 9, 10], p=None))
+            d = int(rng.integers(1, 10 ** min(nd, 6)))
+            if n + d > 2**31 - 1:
+                break
+            n += d
+            s = str(d)
+            if rng.random() < 0.1:
+                s = "0" * int(rng.integers(1, 3)) + s
+            if rng.random() < 0.05:
+                s = s + " "
+            if rng.random() < 0.05:
+                s = s + "\r"
+            parts.append(s)
+            if rng.random() < 0.03:
+                parts.append("")
+    text = "\n".join(parts) + ("\n" if seed % 2 == 0 else "")
+    want = _py_parse(text)
+    out = rs.abcd_remove(text, [], 1)
+    assert _py_parse(out) == want
+    info = rs.plan_abcd(text)
+    allv = [n for v in want.values() for n in v]
+    assert info["num_k"] == len(want) and info["num_candidates"] == len(allv)
+    assert (info["nmin"], info["nmax"]) == (min(allv), max(allv))
+
+
+def test_abcd_parse_large_file(rs):
+    """A file large enough to be read in pieces on several cores: the same
+    sequences as the plain restatement, and an error in a late piece reports
+    the line the serial reader reports."""
+    import numpy as np
+
+    rng = np.random.default_rng(5)
+    parts = []
+    for k in range(3, 3 + 2 * 600, 2):
+        n = int(rng.integers(1, 1000))
+        parts.append(f"ABCD {k}*5^$a-1 [{n}]")
+        d = rng.integers(1, 200, size=int(rng.integers(3000, 9000)))
+        parts.extend(map(str, d.tolist()))
+        if k % 7 == 0:
+            parts.append("")
+    text = "\n".join(parts) + "\n"
+    assert len(text) > 9 * 2**20
+    want = _py_parse(text)
+    allv = [n for v in want.values() for n in v]
+    info = rs.plan_abcd(text)
+    assert info["num_k"] == len(want) and info["num_candidates"] == len(allv)
+    assert (info["nmin"], info["nmax"]) == (min(allv), max(allv))
+    assert _py_parse(rs.abcd_remove(text, [], 1)) == want
+    bad_line = len(parts) - 5
+    broken = "\n".join(parts[: bad_line - 1] + ["x12"] + parts[bad_line:]) + "\n"
+    with pytest.raises(rs.RsieveError) as e:
+        rs.plan_abcd(broken)
+    assert e.value.code == rs.RS_ERR_INVALID and f"line {bad_line}:" in str(e.value)
+
+
 def test_no_cpu_fallback(rs):
     """Without a GPU the library refuses work instead of computing on the CPU."""
     try:
