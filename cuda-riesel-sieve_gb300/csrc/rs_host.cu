@@ -248,9 +248,14 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
   if (np < 2) return parse_abcd_serial(text, len, out);
   std::vector<Seqs> part(np);
   std::vector<int> rc(np, RS_OK);
+  auto piece = [&](size_t t) { rc[t] = parse_abcd_serial(text + cut[t], cut[t + 1] - cut[t], part[t]); };
   std::vector<std::thread> th;
-  for (size_t t = 0; t < np; t++)
-    th.emplace_back([&, t] { rc[t] = parse_abcd_serial(text + cut[t], cut[t + 1] - cut[t], part[t]); });
+  size_t started = 0;
+  try {
+    for (; started < np; started++) th.emplace_back(piece, started);
+  } catch (...) {  // no more threads: the rest run here
+  }
+  for (size_t t = started; t < np; t++) piece(t);
   for (auto &x : th) x.join();
   bool ok = true;
   for (size_t t = 0; t < np; t++)
@@ -535,15 +540,22 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
       fill(0, nk);
     } else {
       // k ranges of about equal candidate counts
-      std::vector<std::thread> th;
+      std::vector<std::pair<size_t, size_t>> ranges;
       size_t k0 = 0, acc = 0;
       for (size_t i = 0; i < nk; i++) {
         acc += s.n[i].size();
-        if (acc * nthr >= ncand * (th.size() + 1) || i + 1 == nk) {
-          th.emplace_back(fill, k0, i + 1);
+        if (acc * nthr >= ncand * (ranges.size() + 1) || i + 1 == nk) {
+          ranges.emplace_back(k0, i + 1);
           k0 = i + 1;
         }
       }
+      std::vector<std::thread> th;
+      size_t started = 0;
+      try {
+        for (; started < ranges.size(); started++) th.emplace_back(fill, ranges[started].first, ranges[started].second);
+      } catch (...) {  // no more threads: the rest run here
+      }
+      for (size_t t = started; t < ranges.size(); t++) fill(ranges[t].first, ranges[t].second);
       for (auto &x : th) x.join();
     }
   }
