@@ -35,6 +35,66 @@ __device__ __forceinline__ uint64_t montmul(uint64_t a, uint64_t b, const Mont &
   return montmul(a, b, m.p, m.pinv);
 }
 
+// The same product as a hand-scheduled inline-PTX chain of 32-bit limbs
+// (mul/mad(c).lo/hi with carry flags, the instruction form of the reference's
+// montmul, kernel_v0.24.6.cu:205-237): t = a*b in four limbs, m = t_lo*pinv mod
+// 2^64 in two, the high half of m*p in two, u = hi(m*p) + t_hi + (t_lo != 0),
+// one masked subtraction.  19 multiply-class instructions.  Same domain and
+// result as montmul(); kept for the measured comparison of the two forms
+// (rs_bench_products) and tested against exact arithmetic (RS_OP_MONTMUL_PTX).
+__device__ __forceinline__ uint64_t montmul_ptx(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv) {
+  uint32_t u0, u1;
+  asm("{\n\t"
+      ".reg .u32 a0, a1, b0, b1, p0, p1, q0, q1, t0, t1, t2, t3, m0, m1, x1, x2, x3, c, v0, v1;\n\t"
+      ".reg .pred nz, neg;\n\t"
+      "mov.b64 {a0, a1}, %2;\n\t"
+      "mov.b64 {b0, b1}, %3;\n\t"
+      "mov.b64 {p0, p1}, %4;\n\t"
+      "mov.b64 {q0, q1}, %5;\n\t"
+      // t = a*b
+      "mul.lo.u32 t0, a0, b0;\n\t"
+      "mul.hi.u32 t1, a0, b0;\n\t"
+      "mad.lo.cc.u32 t1, a0, b1, t1;\n\t"
+      "madc.hi.u32 t2, a0, b1, 0;\n\t"
+      "mad.lo.cc.u32 t1, a1, b0, t1;\n\t"
+      "madc.hi.cc.u32 t2, a1, b0, t2;\n\t"
+      "madc.hi.u32 t3, a1, b1, 0;\n\t"
+      "mad.lo.cc.u32 t2, a1, b1, t2;\n\t"
+      "addc.u32 t3, t3, 0;\n\t"
+      // m = t_lo * pinv mod 2^64
+      "mul.lo.u32 m0, t0, q0;\n\t"
+      "mul.hi.u32 m1, t0, q0;\n\t"
+      "mad.lo.u32 m1, t0, q1, m1;\n\t"
+      "mad.lo.u32 m1, t1, q0, m1;\n\t"
+      // (x3:x2) = high half of m*p (limb 1 only for its carry)
+      "mul.hi.u32 x1, m0, p0;\n\t"
+      "mad.lo.cc.u32 x1, m0, p1, x1;\n\t"
+      "madc.hi.u32 x2, m0, p1, 0;\n\t"
+      "mad.lo.cc.u32 x1, m1, p0, x1;\n\t"
+      "madc.hi.cc.u32 x2, m1, p0, x2;\n\t"
+      "madc.hi.u32 x3, m1, p1, 0;\n\t"
+      "mad.lo.cc.u32 x2, m1, p1, x2;\n\t"
+      "addc.u32 x3, x3, 0;\n\t"
+      // the low halves of t and m*p sum to 0 or 2^64: carry (t_lo != 0)
+      "or.b32 c, t0, t1;\n\t"
+      "setp.ne.u32 nz, c, 0;\n\t"
+      "selp.u32 c, 1, 0, nz;\n\t"
+      "add.cc.u32 x2, x2, t2;\n\t"
+      "addc.u32 x3, x3, t3;\n\t"
+      "add.cc.u32 x2, x2, c;\n\t"
+      "addc.u32 x3, x3, 0;\n\t"
+      // u < 2p: subtract p unless that goes negative
+      "sub.cc.u32 v0, x2, p0;\n\t"
+      "subc.u32 v1, x3, p1;\n\t"
+      "setp.lt.s32 neg, v1, 0;\n\t"
+      "selp.u32 %0, x2, v0, neg;\n\t"
+      "selp.u32 %1, x3, v1, neg;\n\t"
+      "}"
+      : "=r"(u0), "=r"(u1)
+      : "l"(a), "l"(b), "l"(p), "l"(pinv));
+  return ((uint64_t)u1 << 32) | u0;
+}
+
 // x*2^-64 mod p for x < p (leaving Montgomery form): the Montgomery product by 1
 // with its zero high word dropped.  With m = x*pinv mod 2^64, m*p == -x (mod 2^64),
 // so x + m*p = umulhi(m, p)*2^64 + 2^64 when x != 0: the result is

@@ -934,12 +934,14 @@ static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
   };
   const size_t o_raw = sec((size_t)cap * sizeof(Hit)), o_rc = sec(16);
   const size_t o_fac = sec((size_t)cap * sizeof(Hit)), o_fc = sec(16);
+  const size_t o_st = sec(kStatCount * sizeof(unsigned long long));
   CUDA_TRY(cudaMallocAsync(&j->d_hits, off, j->st));
   uint8_t *b = (uint8_t *)j->d_hits;
   j->hb.raw = (Hit *)(b + o_raw);
   j->hb.raw_count = (uint32_t *)(b + o_rc);
   j->hb.fac = (Hit *)(b + o_fac);
   j->hb.fac_count = (uint32_t *)(b + o_fc);
+  j->hb.stat = (unsigned long long *)(b + o_st);
   j->hb.cap = cap;
   return RS_OK;
 }
@@ -972,6 +974,8 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out,
   if (opt.Q < 0 || opt.Q > 4096) return fail(RS_ERR_INVALID, "Q must be in [0, 4096]");
   if (opt.block_scale < 0 || opt.block_scale > 31 || opt.thread_scale < 0 || opt.thread_scale > 31)
     return fail(RS_ERR_INVALID, "-b/-t scale must be in [1, 31]");
+  if (opt.baby_step < RS_BABY_AUTO || opt.baby_step > RS_BABY_HIGH)
+    return fail(RS_ERR_INVALID, "baby_step must be one of RS_BABY_AUTO/SHOUP/SHORT/HIGH");
   Plan pl;
   std::vector<PlanChoice> ranked;
   int rc = make_plan(seqs, opt, pl, true, force, &ranked);
@@ -1108,6 +1112,28 @@ int rs_job_destroy(rs_job *j) {
 
 static constexpr int kRetryHits = -1;
 
+// The baby-step product of a chunk [a, b] (ChunkBufs::small_step).  The short
+// product by the integer b^Q needs p > 2^33 and b^Q * p < 2^63 for every p of
+// the chunk; Shoup's product with a 32-bit constant needs b^Q * 2^32 < p and
+// exists only in the CTA-per-prime kernel; Shoup's full product is always
+// valid.  rs_options.baby_step may prefer a valid form over the cheapest.
+static uint32_t chunk_step_form(const rs_job *j, uint64_t a, uint64_t b) {
+  const uint64_t bq = j->dev.bq_small;
+  const bool small_ok = bq != 0 && a > (1ull << 33) && (unsigned __int128)bq * b < ((unsigned __int128)1 << 63);
+  const bool high_ok = bq != 0 && j->dev.cta_warps > 1 && (bq << 32) < a;
+  switch (j->opt.baby_step) {
+    case RS_BABY_SHOUP: return kStepShoup;
+    case RS_BABY_SHORT:
+      if (small_ok) return kStepSmall;
+      break;
+    case RS_BABY_HIGH:
+      if (high_ok) return kStepHigh;
+      break;
+    default: break;
+  }
+  return small_ok ? kStepSmall : high_ok ? kStepHigh : kStepShoup;
+}
+
 // One pass over [p0, p1]; returns kRetryHits after growing the hit buffers
 // when more candidate hits arrived than they could hold.
 static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
@@ -1137,6 +1163,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
   // chunk list [a, b] with expected prime count ~0.8*C
   struct Chunk {
     uint64_t a, b;
+    uint32_t form;  // baby-step product (chunk_step_form)
   };
   std::vector<Chunk> todo;
   {
@@ -1148,7 +1175,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       if (w > 64.0 * (double)C) w = 64.0 * (double)C;
       uint64_t width = (uint64_t)w & ~1ull;
       uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
-      todo.push_back({a, b});
+      todo.push_back({a, b, 0});
       if (b >= hi) break;
       a = b + 1;
       if (!(a & 1)) a++;
@@ -1187,6 +1214,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
     if (first_pass) {
       cudaMemsetAsync(j->hb.raw_count, 0, 4, j->st);
       cudaMemsetAsync(j->hb.fac_count, 0, 4, j->st);
+      cudaMemsetAsync(j->hb.stat, 0, kStatCount * sizeof(unsigned long long), j->st);
       cudaEventRecord(ev0, j->st);
     }
     for (size_t c = 0; c < todo.size(); c++) {
@@ -1206,17 +1234,8 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
-      {
-        // short baby-step products need p > 2^33 and b^Q * p < 2^63 for every p
-        // of the chunk; Shoup's product with a 32-bit constant needs b^Q * 2^32 < p
-        const uint64_t bq = j->dev.bq_small;
-        if (bq != 0 && todo[c].a > (1ull << 33) && (unsigned __int128)bq * todo[c].b < ((unsigned __int128)1 << 63))
-          j->cb.small_step = kStepSmall;
-        else if (bq != 0 && (bq << 32) < todo[c].a)
-          j->cb.small_step = kStepHigh;
-        else
-          j->cb.small_step = kStepShoup;
-      }
+      todo[c].form = chunk_step_form(j, todo[c].a, todo[c].b);
+      j->cb.small_step = todo[c].form;
       if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
       if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);
       if (timed) cudaEventRecord(evs[6 * c + 3], j->st);
@@ -1264,6 +1283,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
         redo.push_back({mid, todo[c].b});
       } else {
         total_primes += n;
+        st.primes_by_step[todo[c].form == kStepShoup ? 0 : todo[c].form == kStepSmall ? 1 : 2] += n;
       }
     }
     todo.swap(redo);
@@ -1278,14 +1298,18 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
   st.launches += 1;
   cudaEventRecord(ev1, j->st);
   uint32_t counts[2] = {0, 0};
+  unsigned long long dstat[kStatCount] = {};
   if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[0], j->hb.raw_count, 4, cudaMemcpyDeviceToHost, j->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[1], j->hb.fac_count, 4, cudaMemcpyDeviceToHost, j->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dstat, j->hb.stat, sizeof(dstat), cudaMemcpyDeviceToHost, j->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(j->st);
   if (e != cudaSuccess) {
     cleanup_events();
     return fail(RS_ERR_CUDA, "verify: %s", cudaGetErrorString(e));
   }
-  st.d2h_bytes += 8;
+  st.d2h_bytes += 8 + sizeof(dstat);
+  st.paired_primes = dstat[kStatPaired];
+  st.exact_primes = dstat[kStatExact];
   {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
@@ -1524,6 +1548,39 @@ extern "C" int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_
   int rc = check_device(device);
   if (rc) return rc;
   CUDA_TRY(run_imad_bench(device, mul_ops_per_s, montmul_per_s, shoup_per_s));
+  return RS_OK;
+}
+
+extern "C" int rs_bench_products(int device, double *rates) {
+  if (!rates) return fail(RS_ERR_INVALID, "NULL argument");
+  int rc = check_device(device);
+  if (rc) return rc;
+  CUDA_TRY(run_product_bench(device, rates));
+  return RS_OK;
+}
+
+extern "C" int rs_gpu_modmul_check(int32_t op, const uint64_t *a, const uint64_t *b, const uint64_t *c,
+                                   const uint64_t *p, size_t n, uint64_t *out, int device) {
+  if (!a || !b || !c || !p || !out) return fail(RS_ERR_INVALID, "NULL argument");
+  if (op < RS_OP_MONTMUL || op > RS_OP_MONTMUL_PTX) return fail(RS_ERR_INVALID, "unknown operation %d", op);
+  for (size_t i = 0; i < n; i++)
+    if (!(p[i] & 1) || p[i] < 3 || p[i] >= (1ull << 63))
+      return fail(RS_ERR_INVALID, "modmul check modulus %zu out of range", i);
+  if (n == 0) return RS_OK;
+  int rc = check_device(device);
+  if (rc) return rc;
+  void *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, n * 8 * 5));
+  uint64_t *da = (uint64_t *)d, *db = da + n, *dc = db + n, *dp = dc + n, *dout = dp + n;
+  cudaError_t e = cudaMemcpy(da, a, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db, b, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dc, c, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dp, p, n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = run_modmul_check(op, da, db, dc, dp, n, dout);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, n * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(RS_ERR_CUDA, "modmul check: %s", cudaGetErrorString(e));
   return RS_OK;
 }
 

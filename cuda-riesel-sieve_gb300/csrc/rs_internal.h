@@ -149,7 +149,11 @@ struct HitBufs {
   Hit *fac;            // [cap] verified factors
   uint32_t *fac_count; // [1]
   uint32_t cap;
+  unsigned long long *stat;  // [kStatCount] counters of one rs_sieve_range call, zeroed at its start
 };
+constexpr int kStatPaired = 0;  // primes whose giant loop took the (k, 0), (k, 1) row-pair path
+constexpr int kStatExact = 1;   // primes finished by the exact kernel
+constexpr int kStatCount = 2;
 
 // Launchers (rs_kernels.cu).  All enqueue on `st` and return the launch status.
 // Odd primes of [lo, hi] (lo odd) appended to out[] (count may exceed cap).
@@ -175,6 +179,12 @@ cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off,
 int set_error(int code, const char *fmt, ...);
 
 cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
+// rates[6]: mad.lo.u32 per second, then 64-bit modular products per second by
+// montmul, montmul_ptx, shoup_mul, shoup_mul32 and mul_small (rs_selftest.cu).
+constexpr int kProductRates = 6;
+cudaError_t run_product_bench(int device, double *rates);
+cudaError_t run_modmul_check(int op, const uint64_t *a, const uint64_t *b, const uint64_t *c, const uint64_t *p,
+                             size_t n, uint64_t *out);
 cudaError_t run_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
                             uint64_t *out_mm, int32_t *out_j);
 

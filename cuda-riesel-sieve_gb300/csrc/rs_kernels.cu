@@ -808,6 +808,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   const uint64_t *ltab = cb.recs + J.el_tab + lane;  // this lane's B^lane; G^(lane+1) 32 further
 
   uint64_t nBl = 0, nGl = 0;
+  uint32_t npaired = 0;  // primes of this warp that took the row-pair path
   if (first < n) {
     stage_copy(stage0, J, cb, first, J.stage_elems, lane);
     nBl = __ldg(ltab + (size_t)first * J.rec_elems);
@@ -909,6 +910,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         // space known to the compiler.
         uint32_t hA = 0, hB = 0;
         const bool paired = RPI == 1 && cb.small_step == kStepSmall && (cur[kElNact] >> 32);
+        npaired += paired && J.stage_full;
         if constexpr (RM == kRowsIntId) {
           const uint16_t *Rst = reinterpret_cast<const uint16_t *>(cur + J.el_row);
           if (paired && J.stage_full)
@@ -998,6 +1000,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     __syncwarp();
   }
   stage_wait_all();
+  if (lane == 0 && npaired) atomicAdd(&hb.stat[kStatPaired], (unsigned long long)npaired);
 }
 
 typedef void (*BsgsFn)(JobDev, ChunkBufs, HitBufs);
@@ -1259,6 +1262,7 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   const uint32_t rc = *cb.redo_count;
   const uint32_t nr = rc < cb.cap ? rc : cb.cap;
   const uint32_t ngroups = gridDim.x * NG;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && nr) atomicAdd(&hb.stat[kStatExact], (unsigned long long)nr);
 #pragma unroll 1
   for (uint32_t r = blockIdx.x * NG + grp; r < nr; r += ngroups) {
     const uint32_t i = cb.redo[r];
@@ -1424,160 +1428,6 @@ __global__ void verify_kernel(JobDev J, HitBufs hb) {
 cudaError_t launch_verify(const JobDev &job, const HitBufs &hb, cudaStream_t st) {
   const unsigned blocks = (hb.cap + 255) / 256;
   verify_kernel<<<blocks, 256, 0, st>>>(job, hb);
-  return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// Integer-multiply pipe microbenchmarks (roofline denominators).
-
-__global__ void __launch_bounds__(256) imad_kernel(uint32_t iters, uint32_t seed, uint32_t *sink) {
-  uint32_t x0 = seed ^ threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
-  uint32_t x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
-  const uint32_t a = 0x9E3779B9u | 1u, c = seed | 1u;
-#pragma unroll 1
-  for (uint32_t i = 0; i < iters; i++) {
-#pragma unroll
-    for (int u = 0; u < 16; u++) {
-      asm volatile("mad.lo.u32 %0, %0, %8, %9;\n\t"
-                   "mad.lo.u32 %1, %1, %8, %9;\n\t"
-                   "mad.lo.u32 %2, %2, %8, %9;\n\t"
-                   "mad.lo.u32 %3, %3, %8, %9;\n\t"
-                   "mad.lo.u32 %4, %4, %8, %9;\n\t"
-                   "mad.lo.u32 %5, %5, %8, %9;\n\t"
-                   "mad.lo.u32 %6, %6, %8, %9;\n\t"
-                   "mad.lo.u32 %7, %7, %8, %9;\n\t"
-                   : "+r"(x0), "+r"(x1), "+r"(x2), "+r"(x3), "+r"(x4), "+r"(x5), "+r"(x6), "+r"(x7)
-                   : "r"(a), "r"(c));
-    }
-  }
-  const uint32_t r = x0 ^ x1 ^ x2 ^ x3 ^ x4 ^ x5 ^ x6 ^ x7;
-  if (r == 0x12345678u) sink[0] = r;
-}
-
-__global__ void __launch_bounds__(256) montmul_kernel(uint32_t iters, uint64_t p, uint64_t pinv,
-                                                      uint64_t *sink) {
-  const uint64_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t x0 = (t * 0x9E3779B97F4A7C15ull) % p, x1 = (x0 + 1) % p, x2 = (x0 + 2) % p, x3 = (x0 + 3) % p;
-  const uint64_t c = (p >> 1) + 12345;
-#pragma unroll 1
-  for (uint32_t i = 0; i < iters; i++) {
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      x0 = montmul(x0, c, p, pinv);
-      x1 = montmul(x1, c, p, pinv);
-      x2 = montmul(x2, c, p, pinv);
-      x3 = montmul(x3, c, p, pinv);
-    }
-  }
-  const uint64_t r = x0 ^ x1 ^ x2 ^ x3;
-  if (r == 0x123456789ull) sink[0] = r;
-}
-
-static uint64_t host_pinv(uint64_t p) {
-  uint64_t x = p;
-  for (int i = 0; i < 5; i++) x *= 2 - p * x;
-  return (uint64_t)0 - x;
-}
-
-__global__ void __launch_bounds__(256) shoup_kernel(uint32_t iters, uint64_t p, uint64_t w, uint64_t wq,
-                                                    uint64_t *sink) {
-  const uint64_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t x0 = (t * 0x9E3779B97F4A7C15ull) % p, x1 = (x0 + 1) % p, x2 = (x0 + 2) % p, x3 = (x0 + 3) % p;
-#pragma unroll 1
-  for (uint32_t i = 0; i < iters; i++) {
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      x0 = shoup_mul(x0, w, wq, p);
-      x1 = shoup_mul(x1, w, wq, p);
-      x2 = shoup_mul(x2, w, wq, p);
-      x3 = shoup_mul(x3, w, wq, p);
-    }
-  }
-  const uint64_t r = x0 ^ x1 ^ x2 ^ x3;
-  if (r == 0x123456789ull) sink[0] = r;
-}
-
-cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s) {
-  cudaError_t e = cudaSetDevice(device);
-  if (e != cudaSuccess) return e;
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  void *sink = nullptr;
-  e = cudaMalloc(&sink, 64);
-  if (e != cudaSuccess) return e;
-  cudaEvent_t a, b;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
-  const int blocks = sms * 8, threads = 256;
-  float best1 = 1e30f, best2 = 1e30f, best3 = 1e30f;
-  const uint32_t it1 = 2048, it2 = 256;
-  const uint64_t p = 10000000000037ull;  // a prime near 1e13
-  const uint64_t w = (p >> 1) + 12345;
-  const uint64_t wq = (uint64_t)(((unsigned __int128)w << 64) / p);
-  for (int rep = 0; rep < 4; rep++) {
-    float ms = 0;
-    cudaEventRecord(a);
-    imad_kernel<<<blocks, threads>>>(it1, 7u + rep, (uint32_t *)sink);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    cudaEventElapsedTime(&ms, a, b);
-    if (rep && ms < best1) best1 = ms;
-    cudaEventRecord(a);
-    montmul_kernel<<<blocks, threads>>>(it2, p, host_pinv(p), (uint64_t *)sink);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    cudaEventElapsedTime(&ms, a, b);
-    if (rep && ms < best2) best2 = ms;
-    cudaEventRecord(a);
-    shoup_kernel<<<blocks, threads>>>(it2, p, w, wq, (uint64_t *)sink);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    cudaEventElapsedTime(&ms, a, b);
-    if (rep && ms < best3) best3 = ms;
-  }
-  e = cudaGetLastError();
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  cudaFree(sink);
-  if (e != cudaSuccess) return e;
-  const double n1 = (double)blocks * threads * it1 * 16 * 8;
-  const double n2 = (double)blocks * threads * it2 * 8 * 4;
-  *mul_ops_per_s = n1 / (best1 * 1e-3);
-  *montmul_per_s = n2 / (best2 * 1e-3);
-  *shoup_per_s = n2 / (best3 * 1e-3);
-  return cudaSuccess;
-}
-
-// ---------------------------------------------------------------------------
-// Arithmetic self-test.
-
-__global__ void arith_kernel(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
-                             uint64_t *out_mm, int32_t *out_j) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint64_t P = p[i];
-  Mont M;
-  M.p = P;
-  M.pinv = mont_pinv(P);
-  uint64_t one, r2;
-  mont_consts(P, M.pinv, one, r2);
-  const uint64_t am = montmul(a[i], r2, M), bm = montmul(b[i], r2, M);
-  out_mm[i] = montmul(montmul(am, bm, M), 1, M);
-  // character of the low 32 bits of a with respect to P
-  uint32_t k = (uint32_t)a[i];
-  if (k == 0) {
-    out_j[i] = 0;
-    return;
-  }
-  uint32_t e2 = __ffs(k) - 1;
-  uint32_t kodd = k >> e2;
-  const uint64_t rcp = kodd > 1 ? (~0ull) / kodd : 0;  // floor((2^64-1)/kodd) == floor(2^64/kodd) for kodd odd > 1
-  out_j[i] = legendre_k(P, kodd, e2, rcp);
-}
-
-cudaError_t run_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
-                            uint64_t *out_mm, int32_t *out_j) {
-  arith_kernel<<<(unsigned)((n + 255) / 256), 256>>>(a, b, p, n, out_mm, out_j);
   return cudaGetLastError();
 }
 

@@ -24,6 +24,14 @@ RS_ERR_INTERNAL = 7
 RS_ERR_BUSY = 8
 RS_ERR_TIMEOUT = 9
 
+# rs_options.baby_step
+BABY_AUTO, BABY_SHOUP, BABY_SHORT, BABY_HIGH = 0, 1, 2, 3
+
+# rs_gpu_modmul_check operations
+OPS = {"montmul": 0, "from_mont": 1, "shoup_const": 2, "shoup": 3, "shoup32": 4, "shoup_w32": 5,
+       "mul_small": 6, "pinv": 7, "one": 8, "r2": 9, "pow": 10, "montmul_ptx": 11}
+PRODUCT_RATES = ("mad_lo_u32", "montmul", "montmul_ptx", "shoup", "shoup32", "mul_small")
+
 FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u4"), ("n", "<u4")])
 
 # Every entry point declared in include/rsieve.h.
@@ -32,7 +40,7 @@ EXPORTS = (
     "rs_plan_abcd", "rs_job_destroy", "rs_sieve_range", "rs_write_factors", "rs_gpu_primes",
     "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
     "rs_abcd_remove", "rs_server_options_default", "rs_server_create", "rs_server_submit",
-    "rs_server_wait", "rs_server_destroy", "rs_job_autotune",
+    "rs_server_wait", "rs_server_destroy", "rs_job_autotune", "rs_gpu_modmul_check", "rs_bench_products",
 )
 
 
@@ -52,7 +60,7 @@ class Options(ctypes.Structure):
         ("datless", ctypes.c_int32),
         ("host_verify", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("baby_step", ctypes.c_int32),
         ("mem_limit", ctypes.c_uint64),
     ]
 
@@ -97,10 +105,16 @@ class Stats(ctypes.Structure):
         ("bsgs_launches", ctypes.c_uint32),
         ("h2d_bytes", ctypes.c_uint64),
         ("d2h_bytes", ctypes.c_uint64),
+        ("primes_by_step", ctypes.c_uint64 * 3),
+        ("paired_primes", ctypes.c_uint64),
+        ("exact_primes", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["primes_by_step"] = {"shoup": d["primes_by_step"][0], "short": d["primes_by_step"][1],
+                               "high": d["primes_by_step"][2]}
+        return d
 
 
 class ServerOptions(ctypes.Structure):
@@ -154,6 +168,8 @@ def lib():
         L.rs_bench_imad.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_double)]
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
+        L.rs_gpu_modmul_check.argtypes = [i32, vp, vp, vp, vp, sz, vp, ctypes.c_int]
+        L.rs_bench_products.argtypes = [ctypes.c_int, vp]
         L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
         L.rs_abcd_remove.argtypes = [ctypes.c_char_p, sz, vp, sz, u64, vp, sz, ctypes.POINTER(sz)]
         L.rs_job_autotune.argtypes = [vp, u64, u64, u32, ctypes.POINTER(JobInfo)]
@@ -369,3 +385,19 @@ def arith_check(a, b, p, device: int = 0):
     _check(lib().rs_gpu_arith_check(a.ctypes.data, b.ctypes.data, p.ctypes.data, len(a), mm.ctypes.data,
                                     jj.ctypes.data, device))
     return mm, jj
+
+
+def modmul_check(op: str, a, b, c, p, device: int = 0) -> np.ndarray:
+    """out[i] = op(a[i], b[i], c[i], p[i]) on the GPU (rs_gpu_modmul_check); see include/rsieve.h."""
+    arrs = [np.ascontiguousarray([int(x) for x in v], dtype=np.uint64) for v in (a, b, c, p)]
+    out = np.zeros(len(arrs[0]), dtype=np.uint64)
+    _check(lib().rs_gpu_modmul_check(OPS[op], arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data,
+                                     arrs[3].ctypes.data, len(out), out.ctypes.data, device))
+    return out
+
+
+def bench_products(device: int = 0) -> dict:
+    """Measured rates of every product form (rs_bench_products): name -> operations per second."""
+    r = (ctypes.c_double * len(PRODUCT_RATES))()
+    _check(lib().rs_bench_products(device, r))
+    return dict(zip(PRODUCT_RATES, list(r)))

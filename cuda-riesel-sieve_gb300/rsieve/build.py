@@ -20,7 +20,7 @@ CLI = os.path.join(BUILD, "rsieve")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
-CU_SOURCES = ["rs_kernels.cu", "rs_host.cu", "rs_static.cu", "rs_server.cu"]
+CU_SOURCES = ["rs_kernels.cu", "rs_host.cu", "rs_static.cu", "rs_server.cu", "rs_selftest.cu"]
 HEADERS = ["rs_arith.cuh", "rs_internal.h"]
 
 

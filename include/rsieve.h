@@ -45,6 +45,13 @@ extern "C" {
 
 typedef struct rs_job rs_job;
 
+/* rs_options.baby_step: the product by B = b^Q that advances a baby-step chain. */
+#define RS_BABY_AUTO 0   /* the cheapest valid form below */
+#define RS_BABY_SHOUP 1  /* Shoup's product by a full-size constant: valid for every prime */
+#define RS_BABY_SHORT 2  /* the short product by the integer b^Q: p > 2^33 and b^Q * p < 2^63 */
+#define RS_BABY_HIGH 3   /* Shoup's product by a 32-bit constant: b^Q * 2^32 < p, CTA-per-prime
+                            layout only (the warp layout then takes RS_BABY_SHOUP) */
+
 /* One removed candidate: p | k*b^n+sign. */
 typedef struct {
   uint64_t p;
@@ -66,7 +73,11 @@ typedef struct {
   int32_t host_verify;  /* re-verify every factor on the host with 128-bit
                            arithmetic (kernel_v0.24.6.cu:1649-1671); default 1 */
   int32_t device;       /* CUDA device ordinal (the reference hard-codes 0) */
-  int32_t reserved;     /* 0 */
+  int32_t baby_step;    /* form of the baby-step product (no counterpart in the
+                           reference, whose only form is its montmul): RS_BABY_AUTO
+                           picks, per launch, the cheapest form valid for every
+                           prime of it; the others force a form where it is valid
+                           (else AUTO) -- results are identical, only speed differs */
   uint64_t mem_limit;   /* device bytes for the job's per-launch buffers, which set the
                            primes per launch when -b/-t are not given; 0 = 3 GiB */
 } rs_options;
@@ -107,6 +118,11 @@ typedef struct {
   uint32_t bsgs_launches;
   uint64_t h2d_bytes;    /* host->device bytes the call copied */
   uint64_t d2h_bytes;    /* device->host bytes the call copied */
+  uint64_t primes_by_step[3]; /* primes whose baby steps used RS_BABY_SHOUP, _SHORT, _HIGH
+                            (index = form - 1) */
+  uint64_t paired_primes; /* primes whose active rows came in (k, 0), (k, 1) pairs, the
+                            second giant value of each pair formed by the short product by b */
+  uint64_t exact_primes; /* primes finished by the exact (tag, j) table path */
 } rs_stats;
 
 void rs_options_default(rs_options *opt);
@@ -193,11 +209,41 @@ int rs_gpu_primes_static(uint64_t lo, uint64_t hi, const uint32_t *sieve_primes,
  * reference; the roofline of the BSGS kernel is stated against it. */
 int rs_bench_imad(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
 
+/* The same measurement for every product form, rates[RS_BENCH_RATES]: 32-bit
+ * mad.lo per second, then 64-bit modular products per second by the Montgomery
+ * product in 64-bit C (__umul64hi), the same as an inline-PTX 32-bit-limb
+ * carry chain (the reference's instruction form, kernel_v0.24.6.cu:205-237),
+ * Shoup's product by a full-size constant, Shoup's product of a 32-bit operand,
+ * and the short product by a 32-bit integer.  No counterpart in the reference. */
+#define RS_BENCH_RATES 6
+int rs_bench_products(int device, double *rates);
+
 /* Device arithmetic self-test: n Montgomery products and Jacobi symbols on the
  * GPU for the given inputs (results written to out_*), used by the parity
  * tests against the oracle.  a, b < p < 2^63, p odd. */
 int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const uint64_t *p, size_t n,
                        uint64_t *out_mulmod, int32_t *out_jacobi_ap, int device);
+
+/* Device self-test of the modular arithmetic the kernels are built from, one
+ * operation per call on n inputs: out[i] = op(a[i], b[i], c[i], p[i]), p odd,
+ * 3 <= p < 2^63.  No counterpart in the reference, whose montmul
+ * (kernel_v0.24.6.cu:182-270) and modul64 (kernel_v0.24.6.cu:150-179) these
+ * generalise.  The caller keeps every input inside the operation's domain (the
+ * parity tests compare against exact integer arithmetic at the domain edges): */
+#define RS_OP_MONTMUL 0     /* a*b*2^-64 mod p; a < 2^64, b < p */
+#define RS_OP_FROM_MONT 1   /* a*2^-64 mod p; a < p */
+#define RS_OP_SHOUP_CONST 2 /* floor(w*2^64/p) from a = w*2^64 mod p */
+#define RS_OP_SHOUP 3       /* a*b mod p with c = floor(b*2^64/p); a < 2^64, b < p */
+#define RS_OP_SHOUP32 4     /* (a mod 2^32)*b mod p with c = floor(b*2^64/p); b < p */
+#define RS_OP_SHOUP_W32 5   /* a*b mod p with c = floor(b*2^64/p); a < 2^64, b*2^32 < p */
+#define RS_OP_MUL_SMALL 6   /* a*b mod p with c = floor(2^64/p); a < p, 2^33 < p, b*p < 2^63 */
+#define RS_OP_PINV 7        /* -p^-1 mod 2^64 */
+#define RS_OP_ONE 8         /* 2^64 mod p */
+#define RS_OP_R2 9          /* 2^128 mod p */
+#define RS_OP_POW 10        /* a^b mod p; a < p */
+#define RS_OP_MONTMUL_PTX 11 /* RS_OP_MONTMUL by the 32-bit-limb inline-PTX carry chain */
+int rs_gpu_modmul_check(int32_t op, const uint64_t *a, const uint64_t *b, const uint64_t *c, const uint64_t *p,
+                        size_t n, uint64_t *out, int device);
 
 const char *rs_last_error(void);
 const char *rs_version(void);

@@ -28,12 +28,15 @@ def _wide_job():
 
 
 def _both(rs, oracle_mod, base, sign, ks, nlists, p0, p1, datless=False, **opts):
+    """GPU and oracle factor sets of one job on [p0, p1]; st["info"] is the GPU job's plan."""
     job = rs.Job(base=base, sign=sign, ks=ks, nlists=nlists, datless=int(datless), **opts)
     g, st = job.sieve(p0, p1)
+    st["info"] = dict(job.info)
     oj = oracle_mod.Job.from_arrays(base, sign, ks, [np.asarray(x) for x in nlists])
     o, npr = oj.sieve(p0, p1, datless=datless)
     job.close()
     assert st["primes"] == npr
+    assert sum(st["primes_by_step"].values()) == st["primes"]
     return _set(g), _set(o), st
 
 
@@ -82,12 +85,59 @@ def test_plain_small_full(rs, oracle_mod):
 
 
 def test_plain_steady_subwindow(rs, oracle_mod):
-    """A 2e7-wide sub-window of the steady-state workload at 1e13."""
+    """The 1e8-wide sub-window [1e13, 1e13+1e8) of the steady-state workload,
+    complete and datless.  Factors are rare this high (the oracle finds 0 and 1),
+    so the non-empty parity of this exact kernel path is test_benchmark_path_near_2_33."""
     import rsieve.synth as S
 
     b, s, ks, nl = S.plain_job(1)
-    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**13, 10**13 + 2 * 10**7)
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**13, 10**13 + 10**8 - 1, datless=datless)
+        assert g == o
+        assert st["primes"] > 3 * 10**6
+        assert st["primes_by_step"]["short"] == st["primes"] and st["paired_primes"] > st["primes"] // 4
+
+
+# The benchmark job's plan: Q = 2, one warp per prime, integer rows kept in the
+# records (row form 1).  Just above 2^33 its baby steps take the short product
+# by b^Q (the form the benchmark window at 1e13 runs) and factors are still
+# plentiful: the oracle reports 8 / 78 (Riesel, complete / datless) on a 1e7
+# window and 8 Sierpinski factors on a 3e7 window.
+_NEAR_2_33 = 2**33 + 1
+
+
+@pytest.mark.parametrize("sign,datless,width", [(-1, False, 10**7), (-1, True, 10**7), (1, False, 3 * 10**7),
+                                                (1, True, 10**7)])
+def test_benchmark_path_near_2_33(rs, oracle_mod, sign, datless, width):
+    """The benchmark's own kernel path on a window where the oracle reports
+    factors: warp-per-prime BSGS with short baby products, integer rows and,
+    for primes with (b/p) = 1, the row-pair giant path; the counters of
+    rs_stats show that path ran."""
+    import rsieve.synth as S
+
+    b, _, ks, nl = S.plain_job(1)
+    g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, _NEAR_2_33, _NEAR_2_33 + width - 1, datless=datless)
+    info = st["info"]
+    assert (info["Q"], info["warps_per_prime"], info["row_form"]) == (2, 1, 1)
+    assert len(o) >= 5
     assert g == o
+    assert st["primes_by_step"]["short"] == st["primes"]
+    assert st["primes"] // 4 < st["paired_primes"] < st["primes"]
+
+
+@pytest.mark.parametrize("baby_step", ["shoup", "short"])
+def test_benchmark_job_forced_baby_step(rs, oracle_mod, baby_step):
+    """The same window with the baby-step product forced: Shoup's full product
+    (no row pairs, which ride on the short product) and the short one."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    form = {"shoup": rs.BABY_SHOUP, "short": rs.BABY_SHORT}[baby_step]
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, _NEAR_2_33, _NEAR_2_33 + 10**7 - 1, datless=True,
+                     baby_step=form)
+    assert len(o) >= 5 and g == o
+    assert st["primes_by_step"][baby_step] == st["primes"]
+    assert (st["paired_primes"] > 0) == (baby_step == "short")
 
 
 @pytest.mark.parametrize("opts", [{}, {"Q": 18}, {"Q": 2}, {"Q": 18, "hash_m": 5}, {"Q": 6, "hash_m": 9}])
@@ -201,6 +251,25 @@ def test_wide_config_window(rs, oracle_mod):
     assert st["primes"] > 50000
 
 
+@pytest.mark.parametrize("baby_step,datless", [("auto", False), ("auto", True), ("high", True), ("shoup", True)])
+def test_wide_job_near_2_35(rs, oracle_mod, baby_step, datless):
+    """The wide job's own path (16 warps per prime, row ids only) on a window
+    where the oracle reports factors (7 complete, 487 datless on 2e5 at 2^35),
+    with each baby-step product the CTA kernel has: the short product (auto),
+    Shoup's product by the 32-bit constant b^Q (valid: 2 * 2^32 < p) and
+    Shoup's full product."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = _wide_job()
+    form = {"auto": rs.BABY_AUTO, "high": rs.BABY_HIGH, "shoup": rs.BABY_SHOUP}[baby_step]
+    p0 = 2**35 + 1
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**5 - 1, datless=datless, baby_step=form)
+    assert st["info"]["warps_per_prime"] == 16
+    assert len(o) >= 5 and g == o
+    want = {"auto": "short", "high": "high", "shoup": "shoup"}[baby_step]
+    assert st["primes_by_step"][want] == st["primes"]
+
+
 @pytest.mark.parametrize("i", [0, 1, 2, 3])
 def test_batch_shaped_jobs(rs, oracle_mod, i):
     """Jobs drawn from the mixed-batch distribution (random base, k count,
@@ -228,6 +297,11 @@ def test_row_forms(rs, oracle_mod, i, form, wpp):
     assert (info["row_form"], info["warps_per_prime"]) == (form, wpp)
     g, o, st = _both(rs, oracle_mod, b, s, ks, nl, 10**6, 10**6 + 2 * 10**5, datless=True)
     assert g == o and len(o) > 0
+    # just above 2^33, where the faster baby-step products start to apply
+    # (jobs with few k need a wider window for factors)
+    width = 2 * 10**6 if len(ks) < 50 else 2 * 10**5
+    g, o, st = _both(rs, oracle_mod, b, s, ks, nl, _NEAR_2_33, _NEAR_2_33 + width - 1, datless=True)
+    assert g == o and len(o) >= 3
     g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**5, datless=True)
     assert g == o and st["primes"] > 1000
 
@@ -264,6 +338,12 @@ def test_cta_layout_more_giant_steps(rs, oracle_mod, hash_m, sign):
     g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, p0, p0 + 5 * 10**5, hash_m=hash_m)
     assert g == o
     assert st["primes"] > 10000
+    # a window with factors, just above 2^35
+    q0 = 2**35 + 1
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, q0, q0 + 2 * 10**5 - 1, datless=datless, hash_m=hash_m)
+        assert g == o
+    assert len(o) >= 5
 
 
 def test_sierpinski_row_pairs_near_1e13(rs, oracle_mod):
