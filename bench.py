@@ -3,15 +3,21 @@
 Workload ("plain_steady"): base 745, 22 seeded odd k in [3, 1e6], n in
 [180000, 250000] kept at 5%, every prime p in [1e13, 1e13 + 1e11).  One step =
 one 1e10-wide slice of that window through the hot path (device prime sieve ->
-per-prime setup -> BSGS -> verify), so the default 10 timed steps cover the
-whole window once.  Metric p/sec = width of the p-interval sieved per second,
-the reference's definition (kernel_v0.24.6.cu:1552-1554,1783).
+per-prime setup -> BSGS -> verify).  Step i sieves slice i mod 10, so the
+default 10 timed steps cover the whole window once and more steps go round it
+again: every sieved p lies inside the stated window.  Metric p/sec = width of
+the p-interval sieved per second, the reference's definition
+(kernel_v0.24.6.cu:1552-1554,1783).
 
   value  device time: summed CUDA-event time of each rs_sieve_range call, from
          its first kernel to its last, job resident in HBM.
-  e2e    the same through the C ABI from host buffers, per step: create the job
-         from its ABCD text (H2D upload), sieve the slice, copy the factors back
-         (D2H), destroy the job; host wall clock around it.
+  e2e    the same through the C ABI from host buffers, over the same steps and
+         slices: per step, create the job from its ABCD text (H2D upload), sieve
+         the slice, copy the factors back (D2H), destroy the job; host wall
+         clock around it.
+
+--workload wide / sr745 measure the wide job near 2^50 or the reference's own
+file sr_745.abcd from the reference's default low bound instead.
 
 Extra keys: roofline (the BSGS kernel against this GPU's measured integer
 multiply throughput), cpu_baseline (the CPU oracle on a bounded sub-window),
@@ -55,24 +61,56 @@ WORKLOAD = ("plain_steady: b=745, 22 seeded odd k in [3,1e6], n in [180000,25000
             "all primes p in [1e13, 1e13+1e11)")
 JOB = "plain_job"
 
-# --workload wide: the wide-n, many-k job near 2^50 (a parity configuration,
-# measured on request; the default line is the plain steady-state workload)
-WIDE = {
-    "METRIC": "p/sec (b=2, 1000 k, n 1e6–3e6)", "P_START": 1 << 50, "WINDOW": 5 * 10**10, "SLICE": 5 * 10**9,
-    "WORKLOAD": ("wide: b=2, 1000 seeded odd k in [3,1e7], n in [1e6,3e6] at 2% density, "
-                 "all primes p in [2^50, 2^50+5e10)"),
-    "JOB": "wide_job", "PROFILE": "bsgs_cta_kernel.wide.txt",
+# Other workloads, measured on request (the default line is the plain
+# steady-state workload):
+#   wide   the wide-n, many-k job near 2^50
+#   sr745  the reference's own file sr_745.abcd (the file its published p/sec
+#          figures are quoted on, README.md:12-20) from the reference's default
+#          low bound 102297149770000 (kernel_v0.24.6.cu:836)
+WORKLOADS = {
+    "wide": {
+        "METRIC": "p/sec (b=2, 1000 k, n 1e6–3e6)", "P_START": 1 << 50, "WINDOW": 5 * 10**10, "SLICE": 5 * 10**9,
+        "WORKLOAD": ("wide: b=2, 1000 seeded odd k in [3,1e7], n in [1e6,3e6] at 2% density, "
+                     "all primes p in [2^50, 2^50+5e10)"),
+        "JOB": "wide_job", "PROFILE": "bsgs_cta_kernel.wide.txt",
+    },
+    "sr745": {
+        "METRIC": "p/sec (sr_745.abcd: b=745, 22 k, n 182644–250000)", "P_START": 102297149770000,
+        "WINDOW": 10**11, "SLICE": 10**10,
+        "WORKLOAD": ("sr745: the reference's sr_745.abcd (65111 candidates), all primes p in "
+                     "[102297149770000, 102297149770000+1e11)"),
+        "JOB": "sr745", "PROFILE": None,
+    },
 }
 PROFILE = "bsgs_kernel.plain_steady.txt"  # committed ncu summary with the BSGS kernel's DRAM bytes per prime
 
 
 def select_workload(name: str) -> None:
-    if name == "wide":
-        globals().update(WIDE)
+    if name in WORKLOADS:
+        globals().update(WORKLOADS[name])
+
+
+def workload_abcd() -> str:
+    """The workload's job as ABCD text (seeded synthetic, or the reference's own file)."""
+    if JOB == "sr745":
+        with open(os.path.join(ROOT, "tests", "golden", "sr_745.abcd")) as f:
+            return f.read()
+    import rsieve.synth as S
+
+    b, s, ks, nl = getattr(S, JOB)(1)
+    return S.to_abcd(b, s, ks, nl)
+
+
+def slice_start(idx: int, slice_w: int) -> int:
+    """Start of slice idx, wrapped so that every slice lies inside [P_START, P_START + WINDOW)."""
+    per = max(1, WINDOW // slice_w)
+    return P_START + (idx % per) * slice_w
 
 
 def bsgs_bytes_per_prime():
     """DRAM bytes per prime of the BSGS kernel from the committed ncu summary."""
+    if not PROFILE:
+        return None
     path = os.path.join(ROOT, "profiles", PROFILE)
     try:
         for line in open(path):
@@ -182,14 +220,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(job_args, seconds: float = 12.0) -> dict:
-    """The CPU oracle on a sub-window of the workload at 1e13, all host threads."""
-    import numpy as np
-
+def cpu_baseline(abcd: str, seconds: float = 12.0) -> dict:
+    """The CPU oracle on a sub-window of the workload's window, all host threads."""
     import oracle
 
-    b, s, ks, nl = job_args
-    oj = oracle.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    oj = oracle.Job.from_abcd(abcd)
     threads = oracle.default_threads()
     w0 = 2 * 10**6
     t = time.perf_counter()
@@ -207,14 +242,10 @@ def run_reference(args, rank: int) -> None:
     """The reference arm: the CPU oracle (the reference's sieve is CUDA-only)."""
     if rank != 0:
         return
-    import numpy as np
-
     import oracle
-    import rsieve.synth as S
 
     oracle.build()
-    b, s, ks, nl = getattr(S, JOB)(1)
-    oj = oracle.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    oj = oracle.Job.from_abcd(workload_abcd())
     threads = oracle.default_threads()
     # per-step sample sized to ~3 s of CPU work
     w0 = 10**6
@@ -363,7 +394,7 @@ def run_served(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", default="plain", choices=["plain", "wide"])
+    ap.add_argument("--workload", default="plain", choices=["plain"] + sorted(WORKLOADS))
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -391,24 +422,20 @@ def main() -> None:
         run_reference(args, rank)
         return
 
-    import numpy as np
-
     import rsieve
-    import rsieve.synth as S
 
     rsieve.build()
     dist = Dist(world, local, "nccl")
     dev = local
     slice_w = int(args.slice)
-    job_args = getattr(S, JOB)(1)
-    b, s, ks, nl = job_args
-    abcd = S.to_abcd(b, s, ks, nl)
+    abcd = workload_abcd()
 
-    # roofline denominator: this GPU's integer-multiply throughput
-    mul_ops, mont_per_s, shoup_per_s = rsieve.bench_imad(dev)
-    modmul_per_s = max(mont_per_s, shoup_per_s)
+    # roofline denominator: this GPU's measured rate of 64-bit modular products
+    rates = rsieve.bench_products(dev)
+    mul_ops = rates["mad_lo_u32"]
+    modmul_per_s = max(rates["montmul"], rates["montmul_ptx"], rates["shoup"])
 
-    job = rsieve.Job(base=b, sign=s, ks=ks, nlists=nl, device=dev, Q=args.Q, hash_m=args.hash_m)
+    job = rsieve.Job(abcd, device=dev, Q=args.Q, hash_m=args.hash_m)
     info = job.info
     # warm-up: slices just below the window
     for w in range(args.warmup):
@@ -421,9 +448,11 @@ def main() -> None:
     t0 = time.perf_counter()
     gpu_ms = bsgs_ms = setup_ms = sieve_ms = exact_ms = 0.0
     primes = launches = bsgs_launches = factors = 0
+    covered = set()
     for step in range(args.steps):
         idx = step * world + rank
-        a = P_START + idx * slice_w
+        a = slice_start(idx, slice_w)
+        covered.add(a)
         f, st = job.sieve(a, a + slice_w - 1)
         gpu_ms += st["gpu_ms"]
         bsgs_ms += st["bsgs_ms"]
@@ -454,10 +483,10 @@ def main() -> None:
         dist.barrier()
         t0 = time.perf_counter()
         h2d = d2h = 0
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = args.steps
         for step in range(e2e_steps):
             idx = step * world + rank
-            a = P_START + idx * slice_w
+            a = slice_start(idx, slice_w)
             with rsieve.Job(abcd, device=dev, Q=args.Q, hash_m=args.hash_m) as j2:
                 f, st = j2.sieve(a, a + slice_w - 1)
                 h2d += j2.info["upload_bytes"] + st["h2d_bytes"]
@@ -469,7 +498,7 @@ def main() -> None:
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(job_args)
+        cpu = cpu_baseline(abcd)
     dist.close()
     if rank != 0:
         return
@@ -478,7 +507,10 @@ def main() -> None:
         "warmup": args.warmup, "ms_per_step": gpu_ms / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
         "config": {
-            "workload": WORKLOAD, "slice_width": slice_w, "plan": {
+            "workload": WORKLOAD, "slice_width": slice_w,
+            "sieved": (f"{args.steps} slices of {slice_w} per rank, {len(covered)} distinct, all inside "
+                       f"[{P_START}, {P_START + WINDOW})"),
+            "plan": {
                 k: info[k] for k in ("Q", "rows", "x_range", "baby_steps", "giant_steps", "table_slots",
                                      "primes_per_launch", "warps_per_prime")},
             "l2": ("no flush: each step streams the per-prime records of a fresh prime window (GBs, > 129 MB L2); "
@@ -492,10 +524,12 @@ def main() -> None:
             "what": ("32-bit multiply-class ops of the algorithmic BSGS work (2*sqrt(E[R]*X) Montgomery "
                      f"products per prime = {info['work_per_prime']:.0f}, x{MONTMUL_MULS} ops) per second of "
                      "BSGS kernel time"),
-            "peak_source": ("measured this run by rs_bench_imad: the fastest 64-bit modular product on "
-                            f"this GPU from independent chains, max(Montgomery {mont_per_s:.3e}/s, Shoup "
-                            f"{shoup_per_s:.3e}/s) x{MONTMUL_MULS}; plain mad.lo.u32 peak "
+            "peak_source": ("measured this run by rs_bench_products: the fastest 64-bit modular product on "
+                            "this GPU from independent chains, max(Montgomery in C "
+                            f"{rates['montmul']:.3e}/s, Montgomery in inline PTX {rates['montmul_ptx']:.3e}/s, "
+                            f"Shoup {rates['shoup']:.3e}/s) x{MONTMUL_MULS}; plain mad.lo.u32 peak "
                             f"{mul_ops / 1e12:.1f} Tops/s"),
+            "product_rates": rates,
         },
         "e2e": e2e,
         "cpu_baseline": cpu,
