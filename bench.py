@@ -309,7 +309,7 @@ def run_served(args) -> None:
     total_width = n * width
 
     def key(f):
-        return [(int(p), int(k), int(q)) for p, k, q in f]
+        return [(int(x["p"]), int(x["k"]), int(x["n"])) for x in f]
 
     # warm-up: the shared sieving primes up to sqrt of the largest p, module load
     top = max(jobs, key=lambda j: j[2])

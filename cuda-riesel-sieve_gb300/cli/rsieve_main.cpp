@@ -31,14 +31,25 @@ static void usage() {
   printf("-b SCALE : Primes per launch = 128*2^(b-1) * 128*2^(t-1).\n");
   printf("-t SCALE : (see -b).\n");
   printf("-s SCALE : Accepted for compatibility; the device sieve is always complete.\n");
-  printf("-v       : Don't verify: report every n in [nmin,nmax] (datless).\n");
+  printf("-v [X]   : Don't verify: report every n in [nmin,nmax] (datless).\n");
   printf("-w FILE  : After sieving, write FILE: the input ABCD without the candidates whose\n");
   printf("           factors are in the factor file, headers marked \"// Sieved to P1\".\n");
   printf("-A       : Autotune: time the cheapest plans of the cost model on the first part of the\n");
   printf("           range and keep the fastest (replaces hand-tuning -Q/-m/-b/-t).\n");
   printf("-C FILE  : Checkpoint: resume from the p recorded in FILE (if it is for the same\n");
-  printf("           input and P1) and record progress there after every block of launches.\n");
-  printf("-h       : Prints this help\n");
+  printf("           input file contents, P0 and P1) and record progress there after every\n");
+  printf("           block of launches.\n");
+  printf("-h [X]   : Prints this help\n");
+}
+
+// FNV-1a hash of the input text: a checkpoint is only resumed for the same contents.
+static unsigned long long text_hash(const std::string &t) {
+  unsigned long long h = 1469598103934665603ull;
+  for (unsigned char c : t) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
 }
 
 int main(int argc, char **argv) {
@@ -52,7 +63,13 @@ int main(int argc, char **argv) {
   int inp;
   const char *abcd_out = nullptr, *ckpt = nullptr;
   bool autotune = false;
-  while ((inp = getopt(argc, argv, "Ab:hi:m:p:P:Q:O:s:t:vw:C:")) != -1) {
+  // -h and -v take an argument in the reference's getopt string ("h:", "v:",
+  // kernel_v0.24.6.cu:705) whose value is not used; here it is optional, attached
+  // (-v1) or as the next word when that is not an option (-v 1).
+  auto skip_optional_arg = [&]() {
+    if (!optarg && optind < argc && argv[optind][0] != '-') optind++;
+  };
+  while ((inp = getopt(argc, argv, "Ab:h::i:m:p:P:Q:O:s:t:v::w:C:")) != -1) {
     switch (inp) {
       case 'b': block_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
       case 't': thread_scale = (int)strtol(optarg, nullptr, 0); scale_given = true; break;
@@ -72,7 +89,11 @@ int main(int argc, char **argv) {
       }
       case 'O': factor_file = optarg; break;
       case 's': opt.small_prime_scale = (int)strtol(optarg, nullptr, 0); break;
-      case 'v': opt.datless = 1; opt.host_verify = 1; break;
+      case 'v':
+        skip_optional_arg();
+        opt.datless = 1;
+        opt.host_verify = 1;
+        break;
       case 'w': abcd_out = optarg; break;
       case 'C': ckpt = optarg; break;
       case 'A': autotune = true; break;
@@ -122,8 +143,12 @@ int main(int argc, char **argv) {
   }
   rs_job_info info;
   rs_job_info_get(job, &info);
-  printf("The base is %u; %u k-values, %u candidates, n in [%u, %u]\n", info.base, info.num_k,
-         info.num_candidates, info.nmin, info.nmax);
+  if (info.parts > 1)
+    printf("%u (base, sign) groups; the first: base %u; %u k-values and %u candidates in all\n", info.parts,
+           info.base, info.num_k, info.num_candidates);
+  else
+    printf("The base is %u; %u k-values, %u candidates, n in [%u, %u]\n", info.base, info.num_k,
+           info.num_candidates, info.nmin, info.nmax);
   printf("Q=%u. Rows=%u. Range=%u. Baby steps=%u. Giant steps=%u. Table slots=%u. Primes per launch=%u\n\n",
          info.Q, info.rows, info.x_range, info.baby_steps, info.giant_steps, info.table_slots,
          info.primes_per_launch);
@@ -143,25 +168,30 @@ int main(int argc, char **argv) {
            info.Q, info.baby_steps, info.giant_steps, info.warps_per_prime);
   }
 
-  // Resume from a checkpoint of the same input and P1.
+  // Resume from a checkpoint of the same input (path and contents), P0 and P1.
   unsigned long long p = low;
+  const unsigned long long in_hash = text_hash(text);
   if (ckpt) {
     if (FILE *cf = fopen(ckpt, "r")) {
       char line[4096];
-      unsigned long long next = 0, chigh = 0;
+      unsigned long long next = 0, chigh = 0, clow = 0, chash = 0;
       std::string cin;
       while (fgets(line, sizeof(line), cf)) {
         if (!strncmp(line, "next_p=", 7)) next = strtoull(line + 7, nullptr, 10);
         else if (!strncmp(line, "high=", 5)) chigh = strtoull(line + 5, nullptr, 10);
+        else if (!strncmp(line, "low=", 4)) clow = strtoull(line + 4, nullptr, 10);
+        else if (!strncmp(line, "abcd_hash=", 10)) chash = strtoull(line + 10, nullptr, 16);
         else if (!strncmp(line, "abcd=", 5)) {
           cin = line + 5;
           while (!cin.empty() && (cin.back() == '\n' || cin.back() == '\r')) cin.pop_back();
         }
       }
       fclose(cf);
-      if (chigh == high && cin == abcd && next > p) {
+      if (chigh == high && clow == low && cin == abcd && chash == in_hash && next > p) {
         printf("Resuming from checkpoint %s at p=%llu\n", ckpt, next);
         p = next;
+      } else {
+        printf("Checkpoint %s is for another input, range or file contents: starting at P0\n", ckpt);
       }
     }
   }
@@ -170,7 +200,7 @@ int main(int argc, char **argv) {
     std::string tmp = std::string(ckpt) + ".tmp";
     FILE *cf = fopen(tmp.c_str(), "w");
     if (!cf) return;
-    fprintf(cf, "next_p=%llu\nhigh=%llu\nabcd=%s\n", next, high, abcd);
+    fprintf(cf, "next_p=%llu\nlow=%llu\nhigh=%llu\nabcd_hash=%016llx\nabcd=%s\n", next, low, high, in_hash, abcd);
     fclose(cf);
     rename(tmp.c_str(), ckpt);
   };
@@ -198,8 +228,8 @@ int main(int argc, char **argv) {
       return 1;
     }
     for (size_t i = 0; i < cnt; i++)
-      printf("%llu | %u*%u^%u%s\n", (unsigned long long)out[i].p, out[i].k, info.base, out[i].n,
-             info.sign < 0 ? "-1" : "+1");
+      printf("%llu | %u*%u^%u%s\n", (unsigned long long)out[i].p, out[i].k, out[i].b, out[i].n,
+             out[i].c < 0 ? "-1" : "+1");
     if (cnt && rs_write_factors(job, factor_file, out.data(), cnt)) {
       fprintf(stderr, "error: %s\n", rs_last_error());
       rs_job_destroy(job);
@@ -229,7 +259,7 @@ int main(int argc, char **argv) {
   rs_job_destroy(job);
 
   if (abcd_out) {
-    // every factor line of the factor file for this base and sign
+    // every factor line of the factor file (each names its sequence's base and sign)
     std::vector<rs_factor> rm;
     if (FILE *ff = fopen(factor_file, "r")) {
       unsigned long long fp;
@@ -237,9 +267,8 @@ int main(int argc, char **argv) {
       char sg;
       char line[256];
       while (fgets(line, sizeof(line), ff))
-        if (sscanf(line, "%llu | %u*%u^%u%c1", &fp, &fk, &fb, &fn, &sg) == 5 && fb == info.base &&
-            (sg == '-') == (info.sign < 0))
-          rm.push_back(rs_factor{fp, fk, fn});
+        if (sscanf(line, "%llu | %u*%u^%u%c1", &fp, &fk, &fb, &fn, &sg) == 5 && (sg == '-' || sg == '+'))
+          rm.push_back(rs_factor{fp, fk, fn, fb, sg == '-' ? -1 : 1});
       fclose(ff);
     }
     size_t need = 0;

@@ -18,6 +18,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "rs_internal.h"
@@ -72,13 +73,20 @@ static int check_device(int device) {
 // ---------------------------------------------------------------------------
 // ABCD input (kernel_v0.24.6.cu:938-1083): "ABCD k*b^$a-1 [n0]" headers followed
 // by positive n deltas.  Unlike the reference this rejects malformed lines,
-// takes the sign from the header and merges repeated k.
+// takes the base and the sign from each header (the reference uses the first
+// header's base for every k, kernel_v0.24.6.cu:1009-1016, and assumes -1) and
+// merges repeated sequences.
 
+// Sequences of one job part: one base and one sign.  While a file is parsed,
+// seq_base / seq_sign hold each sequence's own base and sign (split_parts then
+// groups the sequences into parts).
 struct Seqs {
   uint32_t base = 0;
   int32_t sign = 0;
   std::vector<uint32_t> k;
   std::vector<std::vector<uint32_t>> n;
+  std::vector<uint32_t> seq_base;
+  std::vector<int32_t> seq_sign;
 };
 
 // One n-delta line "d..d\n" of 1 to 7 digits, read eight bytes at a time: the
@@ -190,11 +198,9 @@ static int parse_abcd_serial(const char *text, size_t len, Seqs &out) {
       if (out.base == 0) {
         out.base = (uint32_t)bv;
         out.sign = sg;
-      } else if (bv != out.base) {
-        return fail(RS_ERR_INVALID, "ABCD line %ld: all sequences must share one base", line);
-      } else if (sg != out.sign) {
-        return fail(RS_ERR_INVALID, "ABCD line %ld: all sequences must share one sign", line);
       }
+      out.seq_base.push_back((uint32_t)bv);
+      out.seq_sign.push_back(sg);
       out.k.push_back((uint32_t)kv);
       out.n.emplace_back();
       out.n.back().push_back((uint32_t)n0);
@@ -217,9 +223,8 @@ static int parse_abcd_serial(const char *text, size_t len, Seqs &out) {
 // Large files are parsed in pieces on the host's cores: the text is cut at
 // "ABCD" header lines into contiguous ranges of about equal size, each range is
 // read by the serial reader into its own sequence list, and the lists are
-// concatenated in order.  Any error (or a base or sign that differs between
-// ranges) re-runs the serial reader on the whole text, so messages and line
-// numbers are those of the serial reader.
+// concatenated in order.  Any error re-runs the serial reader on the whole
+// text, so messages and line numbers are those of the serial reader.
 static int parse_abcd(const char *text, size_t len, Seqs &out) {
   constexpr size_t kPieceBytes = 4u << 20;
   unsigned nthr = std::thread::hardware_concurrency();
@@ -258,8 +263,7 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
   for (size_t t = started; t < np; t++) piece(t);
   for (auto &x : th) x.join();
   bool ok = true;
-  for (size_t t = 0; t < np; t++)
-    ok = ok && rc[t] == RS_OK && part[t].base == part[0].base && part[t].sign == part[0].sign;
+  for (size_t t = 0; t < np; t++) ok = ok && rc[t] == RS_OK;
   if (!ok) {
     out = Seqs();
     return parse_abcd_serial(text, len, out);
@@ -270,14 +274,43 @@ static int parse_abcd(const char *text, size_t len, Seqs &out) {
   for (auto &p : part) nk += p.k.size();
   out.k.reserve(nk);
   out.n.reserve(nk);
+  out.seq_base.reserve(nk);
+  out.seq_sign.reserve(nk);
   for (auto &p : part) {
     out.k.insert(out.k.end(), p.k.begin(), p.k.end());
+    out.seq_base.insert(out.seq_base.end(), p.seq_base.begin(), p.seq_base.end());
+    out.seq_sign.insert(out.seq_sign.end(), p.seq_sign.begin(), p.seq_sign.end());
     for (auto &v : p.n) out.n.push_back(std::move(v));
   }
   return RS_OK;
 }
 
-// Merge repeated k, sort and de-duplicate every n list.
+// Group parsed sequences by (base, sign), in order of first appearance: each
+// group is planned and sieved as one part of the job.
+static std::vector<Seqs> split_parts(Seqs &&all) {
+  std::vector<Seqs> parts;
+  if (all.seq_base.size() != all.k.size()) {  // built from arrays: one base and sign
+    all.seq_base.clear();
+    all.seq_sign.clear();
+    parts.push_back(std::move(all));
+    return parts;
+  }
+  for (size_t i = 0; i < all.k.size(); i++) {
+    size_t g = 0;
+    for (; g < parts.size(); g++)
+      if (parts[g].base == all.seq_base[i] && parts[g].sign == all.seq_sign[i]) break;
+    if (g == parts.size()) {
+      parts.emplace_back();
+      parts.back().base = all.seq_base[i];
+      parts.back().sign = all.seq_sign[i];
+    }
+    parts[g].k.push_back(all.k[i]);
+    parts[g].n.push_back(std::move(all.n[i]));
+  }
+  return parts;
+}
+
+// Merge repeated k, sort and de-duplicate every n list (sequences of one part).
 static void normalise(Seqs &s) {
   Seqs o;
   o.base = s.base;
@@ -583,18 +616,30 @@ struct DevPrimes {
   }
 };
 
-struct rs_job {
-  std::mutex mu;
+// One part of a job: the sequences of one base and one sign, with their own
+// plan, device arrays, kernel configuration and hit buffers.  A job's parts
+// share its stream, sieving primes, prime windows and chunk buffers: each
+// chunk of primes is sieved once and then set up and searched for every part.
+struct Part {
   std::vector<PlanChoice> ranked;  // the planner's feasible choices, cheapest first (for rs_job_autotune)
-  std::shared_ptr<DevPrimes> primes;  // sieving primes in use (d_sp, d_sp_rcp below point into it)
-  rs_options opt;
   Seqs seqs;
   Plan plan;
   JobDev dev{};
-  int device = 0;
-  cudaStream_t st = nullptr;
   void *d_job = nullptr;  // job arrays
   size_t job_bytes = 0;
+  HitBufs hb{};
+  void *d_hits = nullptr;
+  int bsgs_grid = 0;
+  int exact_grid = 0;
+};
+
+struct rs_job {
+  std::mutex mu;
+  std::shared_ptr<DevPrimes> primes;  // sieving primes in use (d_sp, d_sp_rcp below point into it)
+  rs_options opt;
+  std::vector<std::unique_ptr<Part>> parts;
+  int device = 0;
+  cudaStream_t st = nullptr;
   // sieving primes (odd primes <= sp_limit)
   uint64_t sp_limit = 0;
   uint32_t nsp = 0;
@@ -603,16 +648,18 @@ struct rs_job {
   uint64_t gbits_words = 0;
   uint32_t *d_sp = nullptr;
   uint64_t *d_sp_rcp = nullptr;
-  // chunk and hit buffers
+  // chunk buffers (records sized for the largest part)
   ChunkBufs cb{};
   void *d_chunk = nullptr;
-  HitBufs hb{};
-  void *d_hits = nullptr;
   uint32_t *h_counts = nullptr;  // pinned, one slot per chunk + 2
   size_t h_counts_cap = 0;
-  int bsgs_grid = 0;
-  int exact_grid = 0;
   uint32_t chunk_cap = 0;
+  uint32_t chunk_rec_elems = 0;  // record elements the chunk buffers were sized for
+  uint32_t max_rec_elems() const {
+    uint32_t r = 0;
+    for (auto &pt : parts) r = std::max(r, pt->dev.rec_elems);
+    return r;
+  }
 };
 
 
@@ -666,9 +713,9 @@ static uint32_t plan_row_form(const Plan &pl, const Seqs &s, std::vector<uint32_
   return ids ? kRowsIntId : kRowsIntV;
 }
 
-static int upload_job(rs_job *j) {
-  const Plan &pl = j->plan;
-  const Seqs &s = j->seqs;
+static int upload_part(rs_job *j, Part &pt) {
+  const Plan &pl = pt.plan;
+  const Seqs &s = pt.seqs;
   const uint32_t nk = (uint32_t)s.k.size();
   std::vector<uint32_t> kodd(nk), ke2(nk);
   std::vector<uint64_t> krcp(nk);
@@ -725,7 +772,7 @@ static int upload_job(rs_job *j) {
   const size_t o_kj = sec(nk * 4), o_ki = sec(nk * sizeof(KInfo)), o_tk = sec(tab_k.size() * 4);
   const size_t o_to = sec(tab_off.size() * 4);
   const size_t o_jb = sec(twords * 4);
-  j->job_bytes = o_jb;  // bytes uploaded (the character tables are built on the device)
+  pt.job_bytes = o_jb;  // bytes uploaded (the character tables are built on the device)
   std::vector<uint8_t> host(o_jb, 0);
   memcpy(host.data() + o_rr, pl.row_r.data(), pl.row_r.size() * 4);
   memcpy(host.data() + o_rk, pl.row_kidx.data(), pl.row_kidx.size() * 4);
@@ -755,13 +802,13 @@ static int upload_job(rs_job *j) {
   }
   memcpy(host.data() + o_tk, tab_k.data(), tab_k.size() * 4);
   memcpy(host.data() + o_to, tab_off.data(), tab_off.size() * 4);
-  CUDA_TRY(cudaMallocAsync(&j->d_job, off, j->st));
-  CUDA_TRY(cudaMemcpyAsync(j->d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
-  uint8_t *b = (uint8_t *)j->d_job;
+  CUDA_TRY(cudaMallocAsync(&pt.d_job, off, j->st));
+  CUDA_TRY(cudaMemcpyAsync(pt.d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
+  uint8_t *b = (uint8_t *)pt.d_job;
   CUDA_TRY(launch_jacobi_tables((const uint32_t *)(b + o_tk), (const uint32_t *)(b + o_to),
                                 (uint32_t)tab_k.size(), (uint32_t)twords, (uint32_t *)(b + o_jb), j->st));
   CUDA_TRY(cudaStreamSynchronize(j->st));
-  JobDev &d = j->dev;
+  JobDev &d = pt.dev;
   d.base = s.base;
   d.sign = s.sign;
   d.Q = pl.Q;
@@ -896,10 +943,11 @@ static int ensure_gbits(rs_job *j, uint64_t words) {
   return RS_OK;
 }
 
-static size_t chunk_bytes_per_prime(const rs_job *j) { return 8 + 4 + 8 * (size_t)j->dev.rec_elems; }
+static size_t chunk_bytes_per_prime(const rs_job *j) { return 8 + 4 + 8 * (size_t)j->max_rec_elems(); }
 
 static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
-  if (j->d_chunk && j->chunk_cap >= cap) return RS_OK;
+  const uint32_t rec = j->max_rec_elems();
+  if (j->d_chunk && j->chunk_cap >= cap && j->chunk_rec_elems >= rec) return RS_OK;
   if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
   j->d_chunk = nullptr;
   size_t off = 0;
@@ -908,7 +956,7 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
     off = align_up(off + bytes, 256);
     return o;
   };
-  const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * 8 * j->dev.rec_elems);
+  const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * 8 * rec);
   const size_t o_rd = sec((size_t)cap * 4), o_rc = sec(16);
   CUDA_TRY(cudaMallocAsync(&j->d_chunk, off, j->st));
   uint8_t *b = (uint8_t *)j->d_chunk;
@@ -919,13 +967,14 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   j->cb.redo_count = (uint32_t *)(b + o_rc);
   j->cb.cap = cap;
   j->chunk_cap = cap;
+  j->chunk_rec_elems = rec;
   return RS_OK;
 }
 
-static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
-  if (j->d_hits && j->hb.cap >= cap) return RS_OK;
-  if (j->d_hits) cudaFreeAsync(j->d_hits, j->st);
-  j->d_hits = nullptr;
+static int ensure_hit_buffers(rs_job *j, Part &pt, uint32_t cap) {
+  if (pt.d_hits && pt.hb.cap >= cap) return RS_OK;
+  if (pt.d_hits) cudaFreeAsync(pt.d_hits, j->st);
+  pt.d_hits = nullptr;
   size_t off = 0;
   auto sec = [&](size_t bytes) {
     size_t o = off;
@@ -935,24 +984,30 @@ static int ensure_hit_buffers(rs_job *j, uint32_t cap) {
   const size_t o_raw = sec((size_t)cap * sizeof(Hit)), o_rc = sec(16);
   const size_t o_fac = sec((size_t)cap * sizeof(Hit)), o_fc = sec(16);
   const size_t o_st = sec(kStatCount * sizeof(unsigned long long));
-  CUDA_TRY(cudaMallocAsync(&j->d_hits, off, j->st));
-  uint8_t *b = (uint8_t *)j->d_hits;
-  j->hb.raw = (Hit *)(b + o_raw);
-  j->hb.raw_count = (uint32_t *)(b + o_rc);
-  j->hb.fac = (Hit *)(b + o_fac);
-  j->hb.fac_count = (uint32_t *)(b + o_fc);
-  j->hb.stat = (unsigned long long *)(b + o_st);
-  j->hb.cap = cap;
+  CUDA_TRY(cudaMallocAsync(&pt.d_hits, off, j->st));
+  uint8_t *b = (uint8_t *)pt.d_hits;
+  pt.hb.raw = (Hit *)(b + o_raw);
+  pt.hb.raw_count = (uint32_t *)(b + o_rc);
+  pt.hb.fac = (Hit *)(b + o_fac);
+  pt.hb.fac_count = (uint32_t *)(b + o_fc);
+  pt.hb.stat = (unsigned long long *)(b + o_st);
+  pt.hb.cap = cap;
   return RS_OK;
+}
+
+static void free_part_device(rs_job *j, Part &pt) {
+  if (pt.d_job) cudaFreeAsync(pt.d_job, j->st);
+  if (pt.d_hits) cudaFreeAsync(pt.d_hits, j->st);
+  pt.d_job = nullptr;
+  pt.d_hits = nullptr;
 }
 
 static void free_job(rs_job *j) {
   if (!j) return;
   if (j->st) cudaStreamSynchronize(j->st);
   if (j->st) {
-    if (j->d_job) cudaFreeAsync(j->d_job, j->st);
+    for (auto &pt : j->parts) free_part_device(j, *pt);
     if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
-    if (j->d_hits) cudaFreeAsync(j->d_hits, j->st);
     if (j->d_gbits) cudaFreeAsync(j->d_gbits, j->st);
     cudaStreamSynchronize(j->st);
   }
@@ -961,50 +1016,12 @@ static void free_job(rs_job *j) {
   delete j;
 }
 
-static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out,
-                            const PlanChoice *force = nullptr) {
-  if (!out) return fail(RS_ERR_INVALID, "job pointer is NULL");
-  *out = nullptr;
-  rs_options opt;
-  if (optp) opt = *optp;
-  else rs_options_default(&opt);
-  normalise(seqs);
-  if (seqs.sign != -1 && seqs.sign != 1) return fail(RS_ERR_INVALID, "sign must be -1 or +1");
-  if (seqs.base < 2) return fail(RS_ERR_INVALID, "base must be >= 2");
-  if (opt.Q < 0 || opt.Q > 4096) return fail(RS_ERR_INVALID, "Q must be in [0, 4096]");
-  if (opt.block_scale < 0 || opt.block_scale > 31 || opt.thread_scale < 0 || opt.thread_scale > 31)
-    return fail(RS_ERR_INVALID, "-b/-t scale must be in [1, 31]");
-  if (opt.baby_step < RS_BABY_AUTO || opt.baby_step > RS_BABY_HIGH)
-    return fail(RS_ERR_INVALID, "baby_step must be one of RS_BABY_AUTO/SHOUP/SHORT/HIGH");
-  Plan pl;
-  std::vector<PlanChoice> ranked;
-  int rc = make_plan(seqs, opt, pl, true, force, &ranked);
-  if (rc) return rc;
-  rc = check_device(opt.device);
-  if (rc) return rc;
-  rs_job *j = new rs_job();
-  j->ranked = std::move(ranked);
-  j->opt = opt;
-  j->seqs = std::move(seqs);
-  j->plan = std::move(pl);
-  j->device = opt.device;
-  cudaError_t e = cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking);
-  if (e != cudaSuccess) {
-    delete j;
-    return fail(RS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
-  }
-  rc = upload_job(j);
-  if (!rc) {
-    e = bsgs_configure(j->dev, j->device, &j->bsgs_grid, &j->exact_grid);
-    if (e != cudaSuccess) rc = fail(RS_ERR_CUDA, "bsgs_configure: %s", cudaGetErrorString(e));
-  }
-  if (rc) {
-    free_job(j);
-    return rc;
-  }
-  // primes per launch: -b/-t as in the reference (128*2^(b-1) blocks of
-  // 128*2^(t-1) threads, one prime each), else a memory budget of 3 GiB
-  // (larger launches measured 0.6% faster on the benchmark job than 2 GiB).
+// Primes per launch: -b/-t as in the reference (128*2^(b-1) blocks of
+// 128*2^(t-1) threads, one prime each), else a memory budget of 3 GiB for the
+// chunk buffers (larger launches measured 0.6% faster on the benchmark job
+// than 2 GiB).
+static void set_chunk_cap(rs_job *j) {
+  const rs_options &opt = j->opt;
   uint64_t cap;
   if (opt.block_scale > 0 || opt.thread_scale > 0) {
     const int bs = opt.block_scale > 0 ? opt.block_scale : 1, ts = opt.thread_scale > 0 ? opt.thread_scale : 1;
@@ -1016,8 +1033,70 @@ static int create_from_seqs(Seqs &&seqs, const rs_options *optp, rs_job **out,
   }
   cap = std::max<uint64_t>(cap, 4096);
   cap = std::min<uint64_t>(cap, 1u << 23);
-  j->chunk_cap = 0;
   j->cb.cap = (uint32_t)cap;
+}
+
+// Upload and configure one planned part.
+static int make_part(rs_job *j, std::unique_ptr<Part> &pt) {
+  int rc = upload_part(j, *pt);
+  if (!rc) {
+    const cudaError_t e = bsgs_configure(pt->dev, j->device, &pt->bsgs_grid, &pt->exact_grid);
+    if (e != cudaSuccess) rc = fail(RS_ERR_CUDA, "bsgs_configure: %s", cudaGetErrorString(e));
+  }
+  if (rc) free_part_device(j, *pt);
+  return rc;
+}
+
+// A job from parsed sequences: one part per (base, sign).  `force` (a single
+// part only) takes exactly that plan choice.
+static int create_job(Seqs &&all, const rs_options *optp, rs_job **out, const PlanChoice *force = nullptr) {
+  if (!out) return fail(RS_ERR_INVALID, "job pointer is NULL");
+  *out = nullptr;
+  rs_options opt;
+  if (optp) opt = *optp;
+  else rs_options_default(&opt);
+  std::vector<Seqs> groups = split_parts(std::move(all));
+  for (Seqs &g : groups) {
+    normalise(g);
+    if (g.sign != -1 && g.sign != 1) return fail(RS_ERR_INVALID, "sign must be -1 or +1");
+    if (g.base < 2) return fail(RS_ERR_INVALID, "base must be >= 2");
+  }
+  if (groups.empty()) return fail(RS_ERR_INVALID, "job has no sequences");
+  if (force && groups.size() != 1) return fail(RS_ERR_INTERNAL, "a forced plan needs a single-part job");
+  if (opt.Q < 0 || opt.Q > 4096) return fail(RS_ERR_INVALID, "Q must be in [0, 4096]");
+  if (opt.block_scale < 0 || opt.block_scale > 31 || opt.thread_scale < 0 || opt.thread_scale > 31)
+    return fail(RS_ERR_INVALID, "-b/-t scale must be in [1, 31]");
+  if (opt.baby_step < RS_BABY_AUTO || opt.baby_step > RS_BABY_HIGH)
+    return fail(RS_ERR_INVALID, "baby_step must be one of RS_BABY_AUTO/SHOUP/SHORT/HIGH");
+  // plan every part on the host first: a bad input fails before any device work
+  std::vector<std::unique_ptr<Part>> parts;
+  for (Seqs &g : groups) {
+    auto pt = std::make_unique<Part>();
+    const int rc = make_plan(g, opt, pt->plan, true, force, &pt->ranked);
+    if (rc) return rc;
+    pt->seqs = std::move(g);
+    parts.push_back(std::move(pt));
+  }
+  int rc = check_device(opt.device);
+  if (rc) return rc;
+  rs_job *j = new rs_job();
+  j->opt = opt;
+  j->device = opt.device;
+  cudaError_t e = cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete j;
+    return fail(RS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (auto &pt : parts) {
+    rc = make_part(j, pt);
+    if (rc) {
+      free_job(j);
+      return rc;
+    }
+    j->parts.push_back(std::move(pt));
+  }
+  j->chunk_cap = 0;
+  set_chunk_cap(j);
   *out = j;
   return RS_OK;
 }
@@ -1057,7 +1136,7 @@ int rs_job_create_abcd(const char *text, size_t len, const rs_options *opt, rs_j
   Seqs s;
   int rc = parse_abcd(text, len, s);
   if (rc) return rc;
-  return create_from_seqs(std::move(s), opt, job);
+  return create_job(std::move(s), opt, job);
 }
 
 int rs_job_create(uint32_t base, int32_t sign, uint32_t num_k, const uint32_t *k,
@@ -1075,16 +1154,22 @@ int rs_job_create(uint32_t base, int32_t sign, uint32_t num_k, const uint32_t *k
     for (uint32_t v : s.n.back())
       if (v > 0x7fffffffu) return fail(RS_ERR_INVALID, "n exceeds 2^31-1");
   }
-  return create_from_seqs(std::move(s), opt, job);
+  return create_job(std::move(s), opt, job);
 }
 
 int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   if (!j || !info) return fail(RS_ERR_INVALID, "NULL argument");
-  const Plan &pl = j->plan;
-  info->base = j->seqs.base;
-  info->sign = j->seqs.sign;
-  info->num_k = (uint32_t)j->seqs.k.size();
-  info->num_candidates = pl.ncand;
+  const Part &p0 = *j->parts[0];
+  const Plan &pl = p0.plan;
+  memset(info, 0, sizeof(*info));
+  info->base = p0.seqs.base;
+  info->sign = p0.seqs.sign;
+  for (auto &pt : j->parts) {
+    info->num_k += (uint32_t)pt->seqs.k.size();
+    info->num_candidates += pt->plan.ncand;
+    info->upload_bytes += pt->job_bytes;
+  }
+  info->parts = (uint32_t)j->parts.size();
   info->nmin = pl.nmin;
   info->nmax = pl.nmax;
   info->Q = pl.Q;
@@ -1095,9 +1180,8 @@ int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
   info->primes_per_launch = j->cb.cap;
   info->work_per_prime = pl.work_per_prime;
-  info->upload_bytes = j->job_bytes;
   info->warps_per_prime = pl.cta ? kCtaWarps : 1;
-  info->row_form = plan_row_form(pl, j->seqs, nullptr);
+  info->row_form = plan_row_form(pl, p0.seqs, nullptr);
   return RS_OK;
 }
 
@@ -1112,15 +1196,16 @@ int rs_job_destroy(rs_job *j) {
 
 static constexpr int kRetryHits = -1;
 
-// The baby-step product of a chunk [a, b] (ChunkBufs::small_step).  The short
-// product by the integer b^Q needs p > 2^33 and b^Q * p < 2^63 for every p of
-// the chunk; Shoup's product with a 32-bit constant needs b^Q * 2^32 < p and
-// exists only in the CTA-per-prime kernel; Shoup's full product is always
-// valid.  rs_options.baby_step may prefer a valid form over the cheapest.
-static uint32_t chunk_step_form(const rs_job *j, uint64_t a, uint64_t b) {
-  const uint64_t bq = j->dev.bq_small;
+// The baby-step product of a chunk [a, b] for one part (ChunkBufs::small_step).
+// The short product by the integer b^Q needs p > 2^33 and b^Q * p < 2^63 for
+// every p of the chunk; Shoup's product with a 32-bit constant needs
+// b^Q * 2^32 < p and exists only in the CTA-per-prime kernel; Shoup's full
+// product is always valid.  rs_options.baby_step may prefer a valid form over
+// the cheapest.
+static uint32_t chunk_step_form(const rs_job *j, const Part &pt, uint64_t a, uint64_t b) {
+  const uint64_t bq = pt.dev.bq_small;
   const bool small_ok = bq != 0 && a > (1ull << 33) && (unsigned __int128)bq * b < ((unsigned __int128)1 << 63);
-  const bool high_ok = bq != 0 && j->dev.cta_warps > 1 && (bq << 32) < a;
+  const bool high_ok = bq != 0 && pt.dev.cta_warps > 1 && (bq << 32) < a;
   switch (j->opt.baby_step) {
     case RS_BABY_SHOUP: return kStepShoup;
     case RS_BABY_SHORT:
@@ -1134,8 +1219,13 @@ static uint32_t chunk_step_form(const rs_job *j, uint64_t a, uint64_t b) {
   return small_ok ? kStepSmall : high_ok ? kStepHigh : kStepShoup;
 }
 
-// One pass over [p0, p1]; returns kRetryHits after growing the hit buffers
-// when more candidate hits arrived than they could hold.
+// One pass over [p0, p1]; returns kRetryHits after growing a part's hit
+// buffers when more candidate hits arrived than they could hold.
+//
+// Per chunk of primes, on the job's stream: the device sieve writes the
+// chunk's primes, then every part runs its setup, BSGS and exact kernels on
+// them (the chunk buffers are shared, so the parts follow one another).  After
+// the last chunk each part verifies its candidate hits on the device.
 static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
                             size_t *count, rs_stats *stats) {
   *count = 0;
@@ -1154,16 +1244,18 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
   if (rc) return rc;
   rc = ensure_chunk_buffers(j, j->cb.cap);
   if (rc) return rc;
-  if (!j->d_hits) {
-    rc = ensure_hit_buffers(j, 1u << 20);
-    if (rc) return rc;
+  const size_t P = j->parts.size();
+  for (auto &pt : j->parts) {
+    if (!pt->d_hits) {
+      rc = ensure_hit_buffers(j, *pt, P == 1 ? 1u << 20 : 1u << 16);
+      if (rc) return rc;
+    }
   }
   const uint32_t C = j->cb.cap;
 
   // chunk list [a, b] with expected prime count ~0.8*C
   struct Chunk {
     uint64_t a, b;
-    uint32_t form;  // baby-step product (chunk_step_form)
   };
   std::vector<Chunk> todo;
   {
@@ -1175,13 +1267,16 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       if (w > 64.0 * (double)C) w = 64.0 * (double)C;
       uint64_t width = (uint64_t)w & ~1ull;
       uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
-      todo.push_back({a, b, 0});
+      todo.push_back({a, b});
       if (b >= hi) break;
       a = b + 1;
       if (!(a & 1)) a++;
     }
   }
 
+  // timing events per chunk: before and after the sieve, then before setup,
+  // before BSGS, before the exact kernel and after it, for every part
+  const size_t EV = 2 + 4 * P;
   cudaEvent_t ev0, ev1;
   CUDA_TRY(cudaEventCreate(&ev0));
   CUDA_TRY(cudaEventCreate(&ev1));
@@ -1204,22 +1299,25 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
         return fail(RS_ERR_NOMEM, "cudaMallocHost failed");
       }
     }
-    // (re)create timing events: 6 per chunk
-    while (evs.size() < todo.size() * 6) {
+    while (evs.size() < todo.size() * EV) {
       cudaEvent_t e;
       if (cudaEventCreate(&e) != cudaSuccess) break;
       evs.push_back(e);
     }
-    const bool timed = evs.size() >= todo.size() * 6;
+    const bool timed = evs.size() >= todo.size() * EV;
     if (first_pass) {
-      cudaMemsetAsync(j->hb.raw_count, 0, 4, j->st);
-      cudaMemsetAsync(j->hb.fac_count, 0, 4, j->st);
-      cudaMemsetAsync(j->hb.stat, 0, kStatCount * sizeof(unsigned long long), j->st);
+      for (auto &pt : j->parts) {
+        cudaMemsetAsync(pt->hb.raw_count, 0, 4, j->st);
+        cudaMemsetAsync(pt->hb.fac_count, 0, 4, j->st);
+        cudaMemsetAsync(pt->hb.stat, 0, kStatCount * sizeof(unsigned long long), j->st);
+      }
       cudaEventRecord(ev0, j->st);
     }
+    std::vector<uint32_t> forms(todo.size() * P);
     for (size_t c = 0; c < todo.size(); c++) {
+      cudaEvent_t *ce = timed ? &evs[EV * c] : nullptr;
       cudaMemsetAsync(j->cb.count, 0, 4, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 0], j->st);
+      if (ce) cudaEventRecord(ce[0], j->st);
       cudaError_t e = cudaSuccess;
       {
         const int grc = ensure_gbits(j, sieve_bitmap_words(todo[c].a, todo[c].b));
@@ -1230,25 +1328,30 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       }
       e = launch_sieve(todo[c].a, todo[c].b, j->d_sp, j->d_sp_rcp, j->nsp, j->nsp_small, j->d_gbits,
                        j->cb.primes, j->cb.count, C, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 1], j->st);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&j->h_counts[c], j->cb.count, 4, cudaMemcpyDeviceToHost, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 2], j->st);
-      todo[c].form = chunk_step_form(j, todo[c].a, todo[c].b);
-      j->cb.small_step = todo[c].form;
-      if (e == cudaSuccess) e = launch_setup(j->dev, j->cb, j->st);
-      if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 3], j->st);
-      if (e == cudaSuccess) e = launch_bsgs(j->dev, j->cb, j->hb, j->bsgs_grid, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 4], j->st);
-      if (e == cudaSuccess) e = launch_bsgs_exact(j->dev, j->cb, j->hb, j->exact_grid, j->st);
-      if (timed) cudaEventRecord(evs[6 * c + 5], j->st);
+      if (ce) cudaEventRecord(ce[1], j->st);
+      st.launches += j->nsp > j->nsp_small ? 2 : 1;
+      for (size_t q = 0; q < P && e == cudaSuccess; q++) {
+        Part &pt = *j->parts[q];
+        const uint32_t form = chunk_step_form(j, pt, todo[c].a, todo[c].b);
+        forms[c * P + q] = form;
+        j->cb.small_step = form;
+        if (ce) cudaEventRecord(ce[2 + 4 * q], j->st);
+        e = launch_setup(pt.dev, j->cb, j->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(j->cb.redo_count, 0, 4, j->st);
+        if (ce) cudaEventRecord(ce[3 + 4 * q], j->st);
+        if (e == cudaSuccess) e = launch_bsgs(pt.dev, j->cb, pt.hb, pt.bsgs_grid, j->st);
+        if (ce) cudaEventRecord(ce[4 + 4 * q], j->st);
+        if (e == cudaSuccess) e = launch_bsgs_exact(pt.dev, j->cb, pt.hb, pt.exact_grid, j->st);
+        if (ce) cudaEventRecord(ce[5 + 4 * q], j->st);
+        st.launches += 3;
+        st.bsgs_launches += 1;
+      }
       if (e != cudaSuccess) {
         cleanup_events();
         return fail(RS_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
       }
-      st.launches += 4;
-      st.bsgs_launches += 1;
     }
     cudaError_t e = cudaStreamSynchronize(j->st);
     if (e != cudaSuccess) {
@@ -1258,15 +1361,18 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
     st.d2h_bytes += 4 * todo.size();
     if (timed) {
       for (size_t c = 0; c < todo.size(); c++) {
+        const cudaEvent_t *ce = &evs[EV * c];
         float ms = 0;
-        cudaEventElapsedTime(&ms, evs[6 * c + 0], evs[6 * c + 1]);
+        cudaEventElapsedTime(&ms, ce[0], ce[1]);
         st.sieve_ms += ms;
-        cudaEventElapsedTime(&ms, evs[6 * c + 2], evs[6 * c + 3]);
-        st.setup_ms += ms;
-        cudaEventElapsedTime(&ms, evs[6 * c + 3], evs[6 * c + 4]);
-        st.bsgs_ms += ms;
-        cudaEventElapsedTime(&ms, evs[6 * c + 4], evs[6 * c + 5]);
-        st.exact_ms += ms;
+        for (size_t q = 0; q < P; q++) {
+          cudaEventElapsedTime(&ms, ce[2 + 4 * q], ce[3 + 4 * q]);
+          st.setup_ms += ms;
+          cudaEventElapsedTime(&ms, ce[3 + 4 * q], ce[4 + 4 * q]);
+          st.bsgs_ms += ms;
+          cudaEventElapsedTime(&ms, ce[4 + 4 * q], ce[5 + 4 * q]);
+          st.exact_ms += ms;
+        }
       }
     }
     std::vector<Chunk> redo;
@@ -1283,7 +1389,10 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
         redo.push_back({mid, todo[c].b});
       } else {
         total_primes += n;
-        st.primes_by_step[todo[c].form == kStepShoup ? 0 : todo[c].form == kStepSmall ? 1 : 2] += n;
+        for (size_t q = 0; q < P; q++) {
+          const uint32_t f = forms[c * P + q];
+          st.primes_by_step[f == kStepShoup ? 0 : f == kStepSmall ? 1 : 2] += n;
+        }
       }
     }
     todo.swap(redo);
@@ -1293,55 +1402,81 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
     cleanup_events();
     return fail(RS_ERR_INTERNAL, "prime buffer overflow could not be resolved");
   }
-  // verify candidates on the device
-  cudaError_t e = launch_verify(j->dev, j->hb, j->st);
-  st.launches += 1;
+  // verify every part's candidates on the device, then read the counts
+  cudaError_t e = cudaSuccess;
+  for (auto &pt : j->parts) {
+    if (e == cudaSuccess) e = launch_verify(pt->dev, pt->hb, j->st);
+    st.launches += 1;
+  }
   cudaEventRecord(ev1, j->st);
-  uint32_t counts[2] = {0, 0};
-  unsigned long long dstat[kStatCount] = {};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[0], j->hb.raw_count, 4, cudaMemcpyDeviceToHost, j->st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[1], j->hb.fac_count, 4, cudaMemcpyDeviceToHost, j->st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dstat, j->hb.stat, sizeof(dstat), cudaMemcpyDeviceToHost, j->st);
+  std::vector<uint32_t> counts(2 * P, 0);
+  std::vector<unsigned long long> dstat(kStatCount * P, 0);
+  for (size_t q = 0; q < P; q++) {
+    const Part &pt = *j->parts[q];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[2 * q], pt.hb.raw_count, 4, cudaMemcpyDeviceToHost, j->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[2 * q + 1], pt.hb.fac_count, 4, cudaMemcpyDeviceToHost, j->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&dstat[kStatCount * q], pt.hb.stat, kStatCount * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, j->st);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(j->st);
   if (e != cudaSuccess) {
     cleanup_events();
     return fail(RS_ERR_CUDA, "verify: %s", cudaGetErrorString(e));
   }
-  st.d2h_bytes += 8 + sizeof(dstat);
-  st.paired_primes = dstat[kStatPaired];
-  st.exact_primes = dstat[kStatExact];
+  st.d2h_bytes += P * (8 + kStatCount * sizeof(unsigned long long));
   {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
     st.gpu_ms = ms;
   }
   cleanup_events();
-  if (counts[0] > j->hb.cap) {
-    const uint64_t need = std::min<uint64_t>((uint64_t)counts[0] * 2, 1u << 30);
-    rc = ensure_hit_buffers(j, (uint32_t)need);
-    return rc ? rc : kRetryHits;
+  bool regrow = false;
+  for (size_t q = 0; q < P; q++) {
+    Part &pt = *j->parts[q];
+    if (counts[2 * q] > pt.hb.cap) {
+      const uint64_t need = std::min<uint64_t>((uint64_t)counts[2 * q] * 2, 1u << 30);
+      rc = ensure_hit_buffers(j, pt, (uint32_t)need);
+      if (rc) return rc;
+      regrow = true;
+    }
   }
-  std::vector<Hit> fac(counts[1]);
-  if (counts[1]) {
-    CUDA_TRY(cudaMemcpy(fac.data(), j->hb.fac, counts[1] * sizeof(Hit), cudaMemcpyDeviceToHost));
-    st.d2h_bytes += counts[1] * sizeof(Hit);
+  if (regrow) return kRetryHits;
+  struct Fac {
+    uint64_t p;
+    uint32_t k, n, b;
+    int32_t c;
+  };
+  std::vector<Fac> fac;
+  uint64_t raw = 0;
+  for (size_t q = 0; q < P; q++) {
+    const Part &pt = *j->parts[q];
+    raw += counts[2 * q];
+    st.paired_primes += dstat[kStatCount * q + kStatPaired];
+    st.exact_primes += dstat[kStatCount * q + kStatExact];
+    const uint32_t nf = counts[2 * q + 1];
+    if (!nf) continue;
+    std::vector<Hit> h(nf);
+    CUDA_TRY(cudaMemcpy(h.data(), pt.hb.fac, nf * sizeof(Hit), cudaMemcpyDeviceToHost));
+    st.d2h_bytes += nf * sizeof(Hit);
+    for (const Hit &x : h) fac.push_back(Fac{x.p, x.k, x.n, pt.seqs.base, pt.seqs.sign});
   }
-  std::sort(fac.begin(), fac.end(), [](const Hit &a, const Hit &b) {
-    if (a.p != b.p) return a.p < b.p;
-    if (a.k != b.k) return a.k < b.k;
-    return a.n < b.n;
+  std::sort(fac.begin(), fac.end(), [](const Fac &a, const Fac &b) {
+    return std::tie(a.p, a.k, a.n, a.b, a.c) < std::tie(b.p, b.k, b.n, b.b, b.c);
   });
   fac.erase(std::unique(fac.begin(), fac.end(),
-                        [](const Hit &a, const Hit &b) { return a.p == b.p && a.k == b.k && a.n == b.n; }),
+                        [](const Fac &a, const Fac &b) {
+                          return a.p == b.p && a.k == b.k && a.n == b.n && a.b == b.b && a.c == b.c;
+                        }),
             fac.end());
   if (j->opt.host_verify) {
-    for (const Hit &h : fac)
-      if (!host_verify(h.p, h.k, j->seqs.base, h.n, j->seqs.sign))
+    for (const Fac &h : fac)
+      if (!host_verify(h.p, h.k, h.b, h.n, h.c))
         return fail(RS_ERR_INTERNAL, "factor %llu | %u*%u^%u%+d failed host verification",
-                    (unsigned long long)h.p, h.k, j->seqs.base, h.n, j->seqs.sign);
+                    (unsigned long long)h.p, h.k, h.b, h.n, h.c);
   }
   st.primes = total_primes;
-  st.raw_hits = counts[0];
+  st.raw_hits = raw;
   st.factors = fac.size();
   st.p_covered = hi - lo + 1;
   if (stats) *stats = st;
@@ -1351,6 +1486,8 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
     out[i].p = fac[i].p;
     out[i].k = fac[i].k;
     out[i].n = fac[i].n;
+    out[i].b = fac[i].b;
+    out[i].c = fac[i].c;
   }
   return RS_OK;
 }
@@ -1367,79 +1504,67 @@ extern "C" int rs_sieve_range(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *ou
   return fail(RS_ERR_INTERNAL, "candidate-hit buffer overflow could not be resolved");
 }
 
-// Exchange everything but the mutex (and the ranked choices, which belong to the job's input).
-static void swap_job_state(rs_job *a, rs_job *b) {
-  std::swap(a->primes, b->primes);
-  std::swap(a->opt, b->opt);
-  std::swap(a->plan, b->plan);
-  std::swap(a->dev, b->dev);
-  std::swap(a->device, b->device);
-  std::swap(a->st, b->st);
-  std::swap(a->d_job, b->d_job);
-  std::swap(a->job_bytes, b->job_bytes);
-  std::swap(a->sp_limit, b->sp_limit);
-  std::swap(a->nsp, b->nsp);
-  std::swap(a->nsp_small, b->nsp_small);
-  std::swap(a->d_gbits, b->d_gbits);
-  std::swap(a->gbits_words, b->gbits_words);
-  std::swap(a->d_sp, b->d_sp);
-  std::swap(a->d_sp_rcp, b->d_sp_rcp);
-  std::swap(a->cb, b->cb);
-  std::swap(a->d_chunk, b->d_chunk);
-  std::swap(a->hb, b->hb);
-  std::swap(a->d_hits, b->d_hits);
-  std::swap(a->h_counts, b->h_counts);
-  std::swap(a->h_counts_cap, b->h_counts_cap);
-  std::swap(a->bsgs_grid, b->bsgs_grid);
-  std::swap(a->exact_grid, b->exact_grid);
-  std::swap(a->chunk_cap, b->chunk_cap);
-}
-
+// Measured autotuning, part by part: each of the part's cheapest distinct
+// layouts (its own plan first) is built as a single-part job, timed on [p0, p1]
+// by device events, and the fastest part replaces the job's.
 extern "C" int rs_job_autotune(rs_job *j, uint64_t p0, uint64_t p1, uint32_t candidates, rs_job_info *chosen) {
   if (!j) return fail(RS_ERR_INVALID, "NULL job");
   if (candidates == 0) candidates = 3;
   std::lock_guard<std::mutex> lock(j->mu);
-  // distinct layouts among the cheapest modelled choices (the job's own plan is the first)
-  std::vector<PlanChoice> cand;
-  for (const PlanChoice &c : j->ranked) {
-    bool dup = false;
-    for (const PlanChoice &d : cand) dup |= d.Q == c.Q && d.T == c.T && d.m == c.m && d.cta == c.cta;
-    if (!dup) cand.push_back(c);
-    if (cand.size() >= candidates) break;
-  }
   std::vector<rs_factor> out(1 << 16);
-  double best_ms = 0;
-  size_t best_i = 0;
-  for (size_t c = 0; c < cand.size(); c++) {
-    rs_job *t = nullptr;
-    int rc;
-    if (c == 0) {
-      t = j;
-    } else {
-      Seqs copy = j->seqs;
-      rc = create_from_seqs(std::move(copy), &j->opt, &t, &cand[c]);
-      if (rc) return rc;
+  for (size_t q = 0; q < j->parts.size(); q++) {
+    Part &cur = *j->parts[q];
+    std::vector<PlanChoice> cand;
+    for (const PlanChoice &c : cur.ranked) {
+      bool dup = false;
+      for (const PlanChoice &d : cand) dup |= d.Q == c.Q && d.T == c.T && d.m == c.m && d.cta == c.cta;
+      if (!dup) cand.push_back(c);
+      if (cand.size() >= candidates) break;
     }
-    rs_stats st{};
-    size_t cnt = 0;
-    rc = RS_OK;
-    for (int attempt = 0; attempt < 4; attempt++) {
-      rc = sieve_range_impl(t, p0, p1, out.data(), out.size(), &cnt, &st);
-      if (rc != kRetryHits) break;
+    if (cand.size() < 2) continue;
+    double best_ms = 0;
+    rs_job *best = nullptr;
+    for (size_t c = 0; c < cand.size(); c++) {
+      rs_job *t = nullptr;
+      Seqs copy = cur.seqs;
+      int rc = create_job(std::move(copy), &j->opt, &t, &cand[c]);
+      if (rc) {
+        if (best) free_job(best);
+        return rc;
+      }
+      rs_stats st{};
+      size_t cnt = 0;
+      for (int attempt = 0; attempt < 4; attempt++) {
+        rc = sieve_range_impl(t, p0, p1, out.data(), out.size(), &cnt, &st);
+        if (rc != kRetryHits) break;
+      }
+      if (rc == RS_ERR_CAPACITY) rc = RS_OK;  // the timing is what counts here
+      if (rc) {
+        free_job(t);
+        if (best) free_job(best);
+        return rc;
+      }
+      if (!best || st.gpu_ms < best_ms) {
+        if (best) free_job(best);
+        best = t;
+        best_ms = st.gpu_ms;
+      } else {
+        free_job(t);
+      }
     }
-    if (rc == RS_ERR_CAPACITY) rc = RS_OK;  // the timing is what counts here
-    if (rc) {
-      if (t != j) free_job(t);
-      return rc;
-    }
-    if (c == 0 || st.gpu_ms < best_ms) {
-      if (c > 0) swap_job_state(j, t);  // the faster plan moves into the caller's job
-      best_ms = st.gpu_ms;
-      best_i = c;
-    }
-    if (t != j) free_job(t);
+    // the winner's part (planned, uploaded and configured on this device)
+    // moves into the job; its device memory was allocated on the temporary
+    // job's stream, which is synchronised before it is destroyed
+    cudaStreamSynchronize(best->st);
+    std::swap(j->parts[q], best->parts[0]);
+    free_job(best);  // frees the part that was replaced
   }
-  (void)best_i;
+  if (j->d_chunk && j->chunk_rec_elems < j->max_rec_elems()) {
+    cudaFreeAsync(j->d_chunk, j->st);
+    j->d_chunk = nullptr;
+    j->chunk_cap = 0;
+  }
+  set_chunk_cap(j);
   if (chosen) return rs_job_info_get(j, chosen);
   return RS_OK;
 }
@@ -1449,8 +1574,8 @@ extern "C" int rs_write_factors(const rs_job *j, const char *path, const rs_fact
   FILE *fp = fopen(path, "a");
   if (!fp) return fail(RS_ERR_INVALID, "cannot open %s for appending", path);
   for (size_t i = 0; i < count; i++)
-    fprintf(fp, "%llu | %u*%u^%u%s\n", (unsigned long long)f[i].p, f[i].k, j->seqs.base, f[i].n,
-            j->seqs.sign < 0 ? "-1" : "+1");
+    fprintf(fp, "%llu | %u*%u^%u%s\n", (unsigned long long)f[i].p, f[i].k, f[i].b ? f[i].b : j->parts[0]->seqs.base,
+            f[i].n, (f[i].b ? f[i].c : j->parts[0]->seqs.sign) < 0 ? "-1" : "+1");
   const int bad = ferror(fp);
   fclose(fp);
   if (bad) return fail(RS_ERR_INVALID, "write error on %s", path);
@@ -1459,21 +1584,28 @@ extern "C" int rs_write_factors(const rs_job *j, const char *path, const rs_fact
 
 extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp, rs_job_info *info) {
   if (!text || !info) return fail(RS_ERR_INVALID, "NULL argument");
-  Seqs s;
-  int rc = parse_abcd(text, len, s);
+  Seqs all;
+  int rc = parse_abcd(text, len, all);
   if (rc) return rc;
-  normalise(s);
+  std::vector<Seqs> groups = split_parts(std::move(all));
   rs_options opt;
   if (optp) opt = *optp;
   else rs_options_default(&opt);
-  Plan pl;
-  rc = make_plan(s, opt, pl, false);  // the plan's parameters only
-  if (rc) return rc;
   memset(info, 0, sizeof(*info));
+  Plan pl;
+  for (size_t g = 0; g < groups.size(); g++) {
+    normalise(groups[g]);
+    Plan pg;
+    rc = make_plan(groups[g], opt, pg, false);  // the plan's parameters only
+    if (rc) return rc;
+    info->num_k += (uint32_t)groups[g].k.size();
+    info->num_candidates += pg.ncand;
+    if (g == 0) pl = std::move(pg);
+  }
+  const Seqs &s = groups[0];
+  info->parts = (uint32_t)groups.size();
   info->base = s.base;
   info->sign = s.sign;
-  info->num_k = (uint32_t)s.k.size();
-  info->num_candidates = pl.ncand;
   info->nmin = pl.nmin;
   info->nmax = pl.nmax;
   info->Q = pl.Q;
@@ -1617,26 +1749,34 @@ extern "C" int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const ui
 extern "C" int rs_abcd_remove(const char *text, size_t len, const rs_factor *removed, size_t count,
                               uint64_t sieved_to, char *out, size_t cap, size_t *out_len) {
   if (!text || !out_len || (!removed && count) || (!out && cap)) return fail(RS_ERR_INVALID, "NULL argument");
-  Seqs s;
-  int rc = parse_abcd(text, len, s);
+  Seqs all;
+  int rc = parse_abcd(text, len, all);
   if (rc) return rc;
-  normalise(s);
-  std::vector<std::pair<uint32_t, uint32_t>> rm(count);
-  for (size_t i = 0; i < count; i++) rm[i] = {removed[i].k, removed[i].n};
+  std::vector<Seqs> groups = split_parts(std::move(all));
+  // removed (k, n) keyed by base and sign; b == 0 matches every sequence of that k
+  typedef std::tuple<uint32_t, int32_t, uint32_t, uint32_t> Key;  // (b, c, k, n)
+  std::vector<Key> rm(count);
+  for (size_t i = 0; i < count; i++)
+    rm[i] = Key{removed[i].b, removed[i].b ? (removed[i].c < 0 ? -1 : 1) : 0, removed[i].k, removed[i].n};
   std::sort(rm.begin(), rm.end());
   std::string o;
   char buf[160];
-  for (size_t i = 0; i < s.k.size(); i++) {
-    std::vector<uint32_t> keep;
-    for (uint32_t n : s.n[i])
-      if (!std::binary_search(rm.begin(), rm.end(), std::make_pair(s.k[i], n))) keep.push_back(n);
-    if (keep.empty()) continue;
-    snprintf(buf, sizeof(buf), "ABCD %u*%u^$a%s [%u] // Sieved to %llu\n", s.k[i], s.base, s.sign < 0 ? "-1" : "+1",
-             keep[0], (unsigned long long)sieved_to);
-    o += buf;
-    for (size_t t = 1; t < keep.size(); t++) {
-      snprintf(buf, sizeof(buf), "%u\n", keep[t] - keep[t - 1]);
+  for (Seqs &s : groups) {
+    normalise(s);
+    for (size_t i = 0; i < s.k.size(); i++) {
+      std::vector<uint32_t> keep;
+      for (uint32_t n : s.n[i])
+        if (!std::binary_search(rm.begin(), rm.end(), Key{s.base, s.sign, s.k[i], n}) &&
+            !std::binary_search(rm.begin(), rm.end(), Key{0u, 0, s.k[i], n}))
+          keep.push_back(n);
+      if (keep.empty()) continue;
+      snprintf(buf, sizeof(buf), "ABCD %u*%u^$a%s [%u] // Sieved to %llu\n", s.k[i], s.base,
+               s.sign < 0 ? "-1" : "+1", keep[0], (unsigned long long)sieved_to);
       o += buf;
+      for (size_t t = 1; t < keep.size(); t++) {
+        snprintf(buf, sizeof(buf), "%u\n", keep[t] - keep[t - 1]);
+        o += buf;
+      }
     }
   }
   *out_len = o.size();

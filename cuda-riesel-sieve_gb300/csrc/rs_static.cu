@@ -23,20 +23,56 @@ __device__ __align__(256) uint32_t g_static_window_bits[kStaticWindowWords];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_static_mu;
-uint32_t *g_static_ptr[kMaxDevices] = {nullptr};
+struct StaticAddr {
+  unsigned long long ctx_id;  // the context the address belongs to (0: not known)
+  uint32_t *ptr;
+};
+StaticAddr g_static_addr[kMaxDevices] = {};
+
+// Unique id of the current CUDA context (cuCtxGetId, through the runtime's
+// driver entry points so that the library needs no link to libcuda), or 0 when
+// it cannot be had.  A device reset destroys the primary context and the next
+// one gets a new id, which is how a stale cached address is recognised.
+unsigned long long current_context_id() {
+  typedef int (*GetCurrentFn)(void **);
+  typedef int (*GetIdFn)(void *, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void *f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(f);
+  });
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
 
 // Device address of g_static_window_bits on the current device.  The array's
 // name in host code is only a host-side stand-in, so the address is looked up
-// once per device with that device current and cached.
+// with the device current (cudaGetSymbolAddress) on the first call on each
+// device, and again when the device's context has changed since (after a
+// cudaDeviceReset the module is loaded anew and the old address is dead).
 cudaError_t static_window_bits(int device, uint32_t **out) {
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_ptr[device]) {
+  StaticAddr &a = g_static_addr[device];
+  if (!a.ptr || (ctx != 0 && ctx != a.ctx_id)) {
     void *ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_window_bits);
     if (e != cudaSuccess) return e;
-    g_static_ptr[device] = static_cast<uint32_t *>(ptr);
+    a.ptr = static_cast<uint32_t *>(ptr);
+    a.ctx_id = ctx ? ctx : current_context_id();
   }
-  *out = g_static_ptr[device];
+  *out = a.ptr;
   return cudaSuccess;
 }
 

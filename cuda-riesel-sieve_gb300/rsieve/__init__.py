@@ -32,7 +32,8 @@ OPS = {"montmul": 0, "from_mont": 1, "shoup_const": 2, "shoup": 3, "shoup32": 4,
        "mul_small": 6, "pinv": 7, "one": 8, "r2": 9, "pow": 10, "montmul_ptx": 11}
 PRODUCT_RATES = ("mad_lo_u32", "montmul", "montmul_ptx", "shoup", "shoup32", "mul_small")
 
-FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u4"), ("n", "<u4")])
+# rs_factor: p | k*b^n+c
+FACTOR_DTYPE = np.dtype([("p", "<u8"), ("k", "<u4"), ("n", "<u4"), ("b", "<u4"), ("c", "<i4")])
 
 # Every entry point declared in include/rsieve.h.
 EXPORTS = (
@@ -84,6 +85,7 @@ class JobInfo(ctypes.Structure):
         ("upload_bytes", ctypes.c_uint64),
         ("warps_per_prime", ctypes.c_uint32),
         ("row_form", ctypes.c_uint32),
+        ("parts", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

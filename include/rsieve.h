@@ -52,11 +52,13 @@ typedef struct rs_job rs_job;
 #define RS_BABY_HIGH 3   /* Shoup's product by a 32-bit constant: b^Q * 2^32 < p, CTA-per-prime
                             layout only (the warp layout then takes RS_BABY_SHOUP) */
 
-/* One removed candidate: p | k*b^n+sign. */
+/* One removed candidate: p | k*b^n+c. */
 typedef struct {
   uint64_t p;
   uint32_t k;
   uint32_t n;
+  uint32_t b;  /* the sequence's base (each ABCD header carries its own) */
+  int32_t c;   /* -1 (Riesel, k*b^n-1) or +1 (Sierpinski, k*b^n+1) */
 } rs_factor;
 
 /* Controls of the reference CLI (kernel_v0.24.6.cu:705-786), with AUTO = 0. */
@@ -101,6 +103,9 @@ typedef struct {
   uint32_t warps_per_prime; /* 1: a warp per prime; 16: a CTA per prime (large tables) */
   uint32_t row_form;     /* giant-step start values: 0 per-prime residues, 1 the integers
                             k*b^r (all < 2^32) in the records, 2 k*b^r read by row id */
+  uint32_t parts;        /* (base, sign) groups of the input, each planned and searched as
+                            its own part over the same primes; the plan fields above
+                            describe the first part, num_k and num_candidates count all */
 } rs_job_info;
 
 /* Counters and device-timed durations of the last rs_sieve_range call. */
@@ -128,7 +133,10 @@ typedef struct {
 void rs_options_default(rs_options *opt);
 
 /* Parse an ABCD text (kernel_v0.24.6.cu:938-1083), plan the job
- * (kernel_v0.24.6.cu:1086-1255) and upload it (kernel_v0.24.6.cu:1367-1512). */
+ * (kernel_v0.24.6.cu:1086-1255) and upload it (kernel_v0.24.6.cu:1367-1512).
+ * Every header's base and sign are honoured: sequences are grouped by (base,
+ * sign) into parts that share the prime windows (the reference takes the base
+ * of the first header for every k, kernel_v0.24.6.cu:1009-1016). */
 int rs_job_create_abcd(const char *text, size_t len, const rs_options *opt, rs_job **job);
 
 /* Same from arrays: n lists in CSR form (n_offsets[num_k+1]); sign -1 or +1. */
@@ -145,7 +153,7 @@ int rs_job_destroy(rs_job *job);
 
 /* Sieve p in [p0, p1] (inclusive; the reference's while(low < high) loop,
  * kernel_v0.24.6.cu:1537-1770, without its overshoot past P1).  Factors are
- * sorted by (p, k, n).  If more than cap are found, returns RS_ERR_CAPACITY
+ * sorted by (p, k, n, b, c).  If more than cap are found, returns RS_ERR_CAPACITY
  * with *count = the number found (none written).  stats may be NULL. */
 int rs_sieve_range(rs_job *job, uint64_t p0, uint64_t p1, rs_factor *out, size_t cap,
                    size_t *count, rs_stats *stats);
@@ -161,13 +169,15 @@ int rs_sieve_range(rs_job *job, uint64_t p0, uint64_t p1, rs_factor *out, size_t
 int rs_job_autotune(rs_job *job, uint64_t p0, uint64_t p1, uint32_t candidates, rs_job_info *chosen);
 
 /* Append factors in the reference's format "%llu | %d*%d^%d-1\n"
- * (kernel_v0.24.6.cu:1830-1835; "+1" for a Sierpinski job). */
+ * (kernel_v0.24.6.cu:1830-1835), with each factor's own base and sign ("+1"
+ * for a Sierpinski sequence). */
 int rs_write_factors(const rs_job *job, const char *path, const rs_factor *f, size_t count);
 
 /* Sieve-file update (srsieve workflow; the reference only appends factor lines,
  * kernel_v0.24.6.cu:1830-1835): the ABCD text with every (k, n) in `removed`
- * dropped, k with no candidate left omitted, and "// Sieved to <sieved_to>" on
- * each header.  Host only.  RS_ERR_CAPACITY with *out_len = bytes needed when
+ * dropped (matching the sequence's base and sign too, unless the factor's b is
+ * 0), sequences with no candidate left omitted, and "// Sieved to <sieved_to>"
+ * on each header.  Host only.  RS_ERR_CAPACITY with *out_len = bytes needed when
  * cap is too small. */
 int rs_abcd_remove(const char *text, size_t len, const rs_factor *removed, size_t count, uint64_t sieved_to,
                    char *out, size_t cap, size_t *out_len);
@@ -198,7 +208,9 @@ int rs_gpu_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *c
  * (a cudaStream_t; NULL for the legacy default stream) on the current device;
  * results are valid once the stream has reached this point.  The first call on
  * each device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture. */
+ * that device current; make that first call before any stream capture.  The
+ * address is looked up again on the first call after the device's context has
+ * changed (a cudaDeviceReset), so that call too belongs before any capture. */
 int rs_gpu_primes_static(uint64_t lo, uint64_t hi, const uint32_t *sieve_primes, const uint64_t *sieve_rcp,
                          uint32_t n_sieve, uint64_t *out, uint32_t cap, uint32_t *count, void *stream);
 

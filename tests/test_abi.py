@@ -58,8 +58,6 @@ def test_plan_datless_rows(rs):
 @pytest.mark.parametrize("bad", [
     "12\n",
     "ABCD 3*2^$a-1 [10]\n0\n",
-    "ABCD 3*2^$a-1 [10]\nABCD 5*3^$a-1 [10]\n",
-    "ABCD 3*2^$a-1 [10]\nABCD 5*2^$a+1 [10]\n",
     "ABCD x*2^$a-1 [10]\n",
     "ABCD 3*2^$a-1 10\n",
     "",
@@ -202,9 +200,9 @@ def test_abcd_remove_round_trip(rs, oracle_mod, sr745_text):
     removed = [(ks[0], int(job.nlist(0)[0])), (ks[0], int(job.nlist(0)[5])), (ks[3], int(job.nlist(3)[-1]))]
     # a k whose every candidate is removed disappears
     tiny = "ABCD 3*2^$a-1 [10]\n2\nABCD 5*2^$a-1 [11]\n"
-    out_tiny = rs.abcd_remove(tiny, np.array([(0, 5, 11)], dtype=rs.FACTOR_DTYPE), 10**9)
+    out_tiny = rs.abcd_remove(tiny, np.array([(0, 5, 11, 0, 0)], dtype=rs.FACTOR_DTYPE), 10**9)
     assert "5*2" not in out_tiny and out_tiny.startswith("ABCD 3*2^$a-1 [10] // Sieved to 1000000000\n2\n")
-    f = np.array([(0, k, n) for k, n in removed], dtype=rs.FACTOR_DTYPE)
+    f = np.array([(0, k, n, 0, 0) for k, n in removed], dtype=rs.FACTOR_DTYPE)
     out = rs.abcd_remove(sr745_text, f, 6 * 10**12)
     assert out.count("// Sieved to 6000000000000") == 22
     job2 = oracle_mod.Job.from_abcd(out)
@@ -249,3 +247,23 @@ def test_plan_row_forms(rs, sr745_text):
     assert d["row_form"] == 2 and d["giant_steps"] >= 64
     d = rs.plan_abcd(sr745_text)
     assert d["Q"] > 2 and d["row_form"] == 0
+
+
+def test_plan_per_sequence_bases(rs):
+    """Headers with different bases and signs form parts (no longer an error)."""
+    text = ("ABCD 3*2^$a-1 [10]\n2\n4\nABCD 5*10^$a+1 [7]\n3\nABCD 7*2^$a-1 [11]\n1\n"
+            "ABCD 3*10^$a+1 [20]\n5\n")
+    info = rs.plan_abcd(text)
+    assert info["parts"] == 2 and info["num_k"] == 4 and info["num_candidates"] == 9
+    assert (info["base"], info["sign"]) == (2, -1)
+
+
+def test_abcd_remove_per_sequence_bases(rs):
+    """Removal matches each factor's base and sign (b == 0 matches any)."""
+    text = "ABCD 3*2^$a-1 [10]\n2\nABCD 3*10^$a-1 [10]\n2\n"
+    f = np.array([(0, 3, 10, 2, -1)], dtype=rs.FACTOR_DTYPE)
+    out = rs.abcd_remove(text, f, 10**9)
+    assert "ABCD 3*2^$a-1 [12]" in out and "ABCD 3*10^$a-1 [10]" in out
+    f = np.array([(0, 3, 10, 0, 0)], dtype=rs.FACTOR_DTYPE)
+    out = rs.abcd_remove(text, f, 10**9)
+    assert "ABCD 3*2^$a-1 [12]" in out and "ABCD 3*10^$a-1 [12]" in out

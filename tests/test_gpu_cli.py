@@ -15,6 +15,14 @@ pytestmark = pytest.mark.gpu
 LINE = re.compile(r"^(\d+) \| (\d+)\*(\d+)\^(\d+)([-+])1$")
 
 
+def _fnv1a(data: bytes) -> int:
+    """The CLI's checkpoint hash of the input file's contents (64-bit FNV-1a)."""
+    h = 1469598103934665603
+    for c in data:
+        h = ((h ^ c) * 1099511628211) & (2**64 - 1)
+    return h
+
+
 def _factors(path):
     out = []
     for line in open(path):
@@ -56,7 +64,14 @@ def test_cli_checkpoint_resume_and_abcd_update(rs, oracle_mod, tmp_path):
     assert len(full) > 0
     # resume from a checkpoint in the middle: only the second half is sieved
     mid = lo + 17 * 10**6 + 1
-    (tmp_path / "ck").write_text(f"next_p={mid}\nhigh={hi}\nabcd=job.abcd\n")
+    h = _fnv1a((tmp_path / "job.abcd").read_bytes())
+    # a checkpoint of other file contents (or another P0) is not resumed
+    for bad in (f"low={lo}\nabcd_hash={h ^ 1:016x}\n", f"low={lo + 2}\nabcd_hash={h:016x}\n"):
+        (tmp_path / "ck").write_text(f"next_p={mid}\nhigh={hi}\n{bad}abcd=job.abcd\n")
+        r = subprocess.run(base + ["-O", "ignored.txt", "-C", "ck"], capture_output=True, text=True, cwd=tmp_path,
+                           timeout=300)
+        assert r.returncode == 0 and "Resuming" not in r.stdout and "another input" in r.stdout, r.stderr
+    (tmp_path / "ck").write_text(f"next_p={mid}\nlow={lo}\nhigh={hi}\nabcd_hash={h:016x}\nabcd=job.abcd\n")
     r = subprocess.run(base + ["-O", "half.txt", "-C", "ck"], capture_output=True, text=True, cwd=tmp_path,
                        timeout=300)
     assert r.returncode == 0 and "Resuming from checkpoint" in r.stdout, r.stderr

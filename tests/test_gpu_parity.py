@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _set(f):
-    return [(int(a), int(b), int(c)) for a, b, c in f]
+    """(p, k, n) triples of a factor array (rsieve's or the oracle's)."""
+    return [(int(x["p"]), int(x["k"]), int(x["n"])) for x in f]
 
 
 _WIDE = []
@@ -356,3 +357,43 @@ def test_sierpinski_row_pairs_near_1e13(rs, oracle_mod):
         g, o, st = _both(rs, oracle_mod, b, 1, ks, nl, 10**13, 10**13 + 2 * 10**7, datless=datless)
         assert g == o
     assert st["primes"] > 600000
+
+
+def _mixed_file():
+    """Three (base, sign) groups in one ABCD text, interleaved, some k shared
+    between groups: b=745 Riesel (the plain job), b=2 Riesel, b=745 Sierpinski."""
+    import rsieve.synth as S
+
+    b0, _, ks0, nl0 = S.plain_job(1)
+    _, _, ks1, nl1 = S.make_job(11, 2, 12, 3, 10**6, 180000, 250000, 0.05)
+    groups = [(745, -1, ks0, nl0), (2, -1, ks1, nl1), (745, 1, ks0[:6], nl0[:6])]
+    lines = []
+    for i in range(max(len(g[2]) for g in groups)):
+        for b, c, ks, nl in groups:
+            if i < len(ks):
+                lines.append(S.to_abcd(b, c, ks[i:i + 1], nl[i:i + 1]))
+    return "".join(lines), groups
+
+
+@pytest.mark.parametrize("datless", [False, True])
+def test_per_sequence_bases(rs, oracle_mod, datless):
+    """A file whose headers carry different bases and signs (the reference uses
+    the first header's base for every k, kernel_v0.24.6.cu:1009-1016): every
+    sequence is sieved with its own base and sign, each factor names them, and
+    the set equals the oracle's per group, on a window with factors."""
+    text, groups = _mixed_file()
+    p0, p1 = _NEAR_2_33, _NEAR_2_33 + 10**7 - 1
+    with rs.Job(text, datless=int(datless)) as job:
+        assert job.info["parts"] == 3
+        assert job.info["num_k"] == sum(len(g[2]) for g in groups)
+        g, st = job.sieve(p0, p1)
+    got = [(int(x["p"]), int(x["k"]), int(x["n"]), int(x["b"]), int(x["c"])) for x in g]
+    want = []
+    npr = 0
+    for b, c, ks, nl in groups:
+        oj = oracle_mod.Job.from_arrays(b, c, ks, [np.asarray(x) for x in nl])
+        o, npr = oj.sieve(p0, p1, datless=datless)
+        want += [(int(x["p"]), int(x["k"]), int(x["n"]), b, c) for x in o]
+    assert st["primes"] == npr
+    assert got == sorted(want)
+    assert len({(b, c) for *_, b, c in got}) == 3 if datless else len(got) >= 5

@@ -27,7 +27,7 @@ def _mix(sr745_text):
 
 
 def _key(f):
-    return [(int(p), int(k), int(n)) for p, k, n in f]
+    return [(int(x["p"]), int(x["k"]), int(x["n"])) for x in f]
 
 
 def test_server_results_match_standalone(rs, sr745_text):
