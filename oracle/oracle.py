@@ -89,6 +89,10 @@ def lib():
         L.orc_verify.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                  ctypes.c_int32]
         L.orc_jacobi.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_sieve_ref.argtypes = [ctypes.POINTER(_Job), ctypes.POINTER(_RefPlan), ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+                                    ctypes.POINTER(ctypes.c_uint64)]
         L.orc_default_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -173,6 +177,34 @@ class Job:
             rk = [pl.row_k[i] for i in range(pl.minSubs)]
             rr = [pl.row_r[i] for i in range(pl.minSubs)]
             return RefPlan(pl.minQ, pl.minSubs, pl.minRange, pl.minWork, pl.tMin, pl.tMax, rk, rr)
+        finally:
+            lib().orc_refplan_free(ctypes.byref(pl))
+
+    def sieve_ref(self, p0: int, p1: int, Qin: int = 0, hash_m: int = 8, small_prime_scale: int = 256,
+                  verify: bool = True, threads: int = 0):
+        """Reference projection (orc_sieve_ref): the factor lines one run of the
+        reference executable with -Q Qin -m hash_m -s small_prime_scale (and -v when
+        verify is False) would write for [p0, p1].  Returns (structured array of
+        (p,k,n), number of candidate q tested)."""
+        hash_elems = 2 << hash_m
+        pl = _RefPlan()
+        rc = lib().orc_ref_plan(ctypes.byref(self._j), Qin, hash_elems, ctypes.byref(pl))
+        if rc:
+            raise MemoryError("orc_ref_plan failed")
+        try:
+            cap = 1 << 14
+            while True:
+                out = np.zeros(cap, dtype=FACTOR_DTYPE)
+                cnt = ctypes.c_size_t(0)
+                nc = ctypes.c_uint64(0)
+                rc = lib().orc_sieve_ref(ctypes.byref(self._j), ctypes.byref(pl), hash_elems, small_prime_scale,
+                                         p0, p1, int(verify), threads, out.ctypes.data, cap, ctypes.byref(cnt),
+                                         ctypes.byref(nc))
+                if rc:
+                    raise ValueError("orc_sieve_ref: arguments outside its domain (Riesel, p0 > b, p0 > k)")
+                if cnt.value <= cap:
+                    return out[: cnt.value], nc.value
+                cap = cnt.value
         finally:
             lib().orc_refplan_free(ctypes.byref(pl))
 

@@ -681,3 +681,224 @@ int orc_sieve(const orc_job *job, uint64_t p0, uint64_t p1, int32_t datless, int
   free(primes);
   return bad ? 4 : 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Reference projection: what the reference executable would write.          */
+/*                                                                           */
+/* Restates, on the CPU, the observable behaviour of one reference run:      */
+/*  - its prime source (kernel_v0.24.6.cu:1271-1303, 1838-1987): every odd q  */
+/*    in range with no factor among the first 4096*s odd primes, so that     */
+/*    composites appear above smallP_max^2;                                  */
+/*  - its per-prime search (kernel_v0.24.6.cu:288-620) with its plan (Q,     */
+/*    rows in its sorted order, tMin/tMax for m = hash_elems): B = b^Q,      */
+/*    c1 = B^m, beta = c1^tMin; per row the character filter on (k/q) and    */
+/*    (kb/q), the catch-up by b from the previous row of the same k, giant   */
+/*    steps t in [tMin, tMax) compared with the baby steps B^j, j < m (the   */
+/*    smallest j when several match); a hit of the last t with a match in a */
+/*    row is kept, and the last row with a hit is the prime's one report;    */
+/*  - its host filter (kernel_v0.24.6.cu:1605-1732): n in [minN, maxN]      */
+/*    (its parse quirks), then with verify the candidate bit of the first    */
+/*    row at or after k's first row whose residue is n mod Q (which can be   */
+/*    another k's row) and k*b^n == 1 mod q; without verify every in-range   */
+/*    report is written.                                                     */
+/* The reference's hash-chain edge cases (an all-zero chain word, pointer    */
+/* 0x7FFF) are not emulated.  Riesel only, q > b and q > every k (so that    */
+/* the reference's Legendre routine is the Jacobi symbol).                   */
+
+typedef struct {
+  const orc_job *job;
+  const orc_refplan *pl;
+  uint32_t m;              /* baby steps = hash_elems */
+  int32_t verify;
+  const uint32_t *row_ki;  /* job index of each row's k */
+  const uint64_t *cand;
+  size_t lo, hi;
+  fvec out;
+} rjob;
+
+/* smallest j < m with B^j == y, from a table of (value, j) with linear probing */
+typedef struct {
+  uint64_t *key;
+  uint32_t *val;
+  uint8_t *used;
+  uint32_t bits;
+} btab;
+
+static void ref_prime(rjob *rj, btab *tb, uint64_t q) {
+  const orc_job *job = rj->job;
+  const orc_refplan *pl = rj->pl;
+  const uint32_t m = rj->m, Q = (uint32_t)pl->minQ;
+  mctx c;
+  mctx_init(&c, q);
+  const uint64_t H = (uint64_t)1 << tb->bits, hmask = H - 1;
+  memset(tb->used, 0, H);
+  const uint64_t bm = to_m(&c, job->base);
+  uint64_t B = c.r1;
+  for (uint32_t i = 0; i < Q; i++) B = mmul(&c, B, bm);
+  uint64_t v = c.r1;
+  for (uint32_t j = 0; j < m; j++) {
+    uint64_t h = (v * 0x9E3779B97F4A7C15ull) >> (64 - tb->bits);
+    int dup = 0;
+    while (tb->used[h]) {
+      if (tb->key[h] == v) { dup = 1; break; }
+      h = (h + 1) & hmask;
+    }
+    if (!dup) { tb->used[h] = 1; tb->key[h] = v; tb->val[h] = j; }
+    v = mmul(&c, v, B);
+  }
+  uint64_t c1 = c.r1;
+  for (uint32_t j = 0; j < m; j++) c1 = mmul(&c, c1, B);
+  uint64_t beta = c.r1;
+  for (int32_t t = 0; t < pl->tMin; t++) beta = mmul(&c, beta, c1);
+  const int legb = orc_jacobi(job->base, q) == 1;
+  int32_t rep_k = -1, rep_n = 0;
+  uint32_t lastk = 0;
+  int leg1 = 0, leg2 = 0;
+  uint64_t fb = 0;
+  int32_t prev = 0;
+  for (int32_t row = 0; row < pl->minSubs; row++) {
+    const uint32_t k = (uint32_t)pl->row_k[row];
+    const int32_t r = pl->row_r[row];
+    if (row == 0 || k != lastk) {
+      leg1 = orc_jacobi(k, q) == 1;
+      leg2 = leg1 == legb;
+      fb = mmul(&c, to_m(&c, k), beta);
+      prev = 0;
+    }
+    lastk = k;
+    if (!(leg1 || leg2)) continue;
+    if (!((r % 2 == 0 && leg1) || (r % 2 == 1 && leg2))) continue;
+    for (int32_t t = prev; t < r; t++) fb = mmul(&c, fb, bm);
+    prev = r;
+    uint64_t sB = fb;
+    int32_t output = -1;
+    for (int32_t t = pl->tMin; t < pl->tMax; t++) {
+      sB = mmul(&c, sB, c1);
+      uint64_t h = (sB * 0x9E3779B97F4A7C15ull) >> (64 - tb->bits);
+      while (tb->used[h]) {
+        if (tb->key[h] == sB) { output = (t + 1) * (int32_t)m - (int32_t)tb->val[h]; break; }
+        h = (h + 1) & hmask;
+      }
+    }
+    if (output > 0) { rep_k = (int32_t)k; rep_n = output * (int32_t)Q + r; }
+  }
+  if (rep_k < 0) return;
+  const int32_t n = rep_n;
+  if (!(n > job->ref_minN - 1 && n < job->ref_maxN + 1)) return;
+  if (rj->verify) {
+    const int32_t mod = n % (int32_t)Q;
+    const int32_t idx = (n - mod) / (int32_t)Q - pl->minimum;
+    int32_t row = -1;
+    for (int32_t a = 0; a < pl->minSubs; a++)
+      if (pl->row_k[a] == rep_k) { row = a; break; }
+    if (row < 0) return;
+    while (row < pl->minSubs && pl->row_r[row] != mod) row++;
+    if (row >= pl->minSubs) return; /* past the reference's matrix: not emulated */
+    /* candidate bit idx of that row: n' = (idx + minimum)*Q + r of the row's own k */
+    const int64_t n2 = ((int64_t)idx + pl->minimum) * Q + pl->row_r[row];
+    if (n2 < 0 || n2 > 0x7fffffff || !has_candidate(job, rj->row_ki[row], (uint32_t)n2)) return;
+    if (!orc_verify(q, (uint32_t)rep_k, job->base, (uint32_t)n, -1)) return;
+  }
+  fpush(&rj->out, q, (uint32_t)rep_k, (uint32_t)n);
+}
+
+static void *ref_worker(void *arg) {
+  rjob *rj = (rjob *)arg;
+  btab tb;
+  tb.bits = 1;
+  while (((uint64_t)1 << tb.bits) < 2ull * rj->m) tb.bits++;
+  const size_t H = (size_t)1 << tb.bits;
+  tb.key = (uint64_t *)malloc(H * sizeof(uint64_t));
+  tb.val = (uint32_t *)malloc(H * sizeof(uint32_t));
+  tb.used = (uint8_t *)malloc(H);
+  for (size_t i = rj->lo; i < rj->hi; i++) ref_prime(rj, &tb, rj->cand[i]);
+  free(tb.key);
+  free(tb.val);
+  free(tb.used);
+  return NULL;
+}
+
+/* Odd q in [lo, hi] with no factor among the first nsmall odd primes. */
+static size_t ref_candidates(uint64_t lo, uint64_t hi, const uint32_t *sp, size_t nsp, uint64_t **out) {
+  const uint64_t cnt = (hi - lo) / 2 + 1;
+  char *mark = (char *)calloc(cnt, 1);
+  if (!mark) return 0;
+  for (size_t t = 0; t < nsp; t++) {
+    const uint64_t q = sp[t];
+    uint64_t r = lo % q, f = r ? lo + (q - r) : lo;
+    if (!(f & 1)) f += q;
+    for (uint64_t x = (f - lo) / 2; x < cnt; x += q) mark[x] = 1;
+  }
+  size_t n = 0;
+  for (uint64_t x = 0; x < cnt; x++) n += !mark[x];
+  *out = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  size_t w = 0;
+  for (uint64_t x = 0; x < cnt; x++)
+    if (!mark[x]) (*out)[w++] = lo + 2 * x;
+  free(mark);
+  return n;
+}
+
+int orc_sieve_ref(const orc_job *job, const orc_refplan *pl, int32_t hash_elems, int32_t small_prime_scale,
+                  uint64_t p0, uint64_t p1, int32_t verify, int32_t nthreads, orc_factor *out, size_t cap,
+                  size_t *count, uint64_t *ncand) {
+  *count = 0;
+  if (ncand) *ncand = 0;
+  if (job->sign != -1 || hash_elems < 1 || small_prime_scale < 1 || pl->minSubs < 1) return 1;
+  uint32_t kmax = 0;
+  for (uint32_t i = 0; i < job->nk; i++)
+    if (job->k[i] > kmax) kmax = job->k[i];
+  uint64_t lo = p0 % 2 ? p0 : p0 - 1; /* the reference moves an even low down by one */
+  if (lo <= job->base || lo <= kmax || p1 >= ((uint64_t)1 << 63) || p1 < lo) return 1;
+  /* the first 4096*s odd primes */
+  const size_t want = (size_t)4096 * (size_t)small_prime_scale;
+  const double lw = log((double)want + 10.0);
+  size_t nsp = 0;
+  uint32_t *sp = small_primes((uint64_t)((double)want * (lw + log(lw)) + 1000.0), &nsp);
+  if (nsp > want) nsp = want;
+  uint64_t *cand = NULL;
+  const size_t nc = ref_candidates(lo, p1, sp, nsp, &cand);
+  free(sp);
+  if (ncand) *ncand = nc;
+  uint32_t *row_ki = (uint32_t *)malloc((size_t)pl->minSubs * sizeof(uint32_t));
+  for (int32_t a = 0; a < pl->minSubs; a++) {
+    row_ki[a] = 0;
+    for (uint32_t i = 0; i < job->nk; i++)
+      if ((int32_t)job->k[i] == pl->row_k[a]) { row_ki[a] = i; break; }
+  }
+  int nt = nthreads > 0 ? nthreads : orc_default_threads();
+  if ((size_t)nt > nc) nt = nc ? (int)nc : 1;
+  rjob *rj = (rjob *)calloc(nt, sizeof(rjob));
+  pthread_t *th = (pthread_t *)calloc(nt, sizeof(pthread_t));
+  for (int t = 0; t < nt; t++) {
+    rj[t].job = job;
+    rj[t].pl = pl;
+    rj[t].m = (uint32_t)hash_elems;
+    rj[t].verify = verify;
+    rj[t].row_ki = row_ki;
+    rj[t].cand = cand;
+    rj[t].lo = nc * (size_t)t / nt;
+    rj[t].hi = nc * (size_t)(t + 1) / nt;
+    pthread_create(&th[t], NULL, ref_worker, &rj[t]);
+  }
+  size_t total = 0;
+  for (int t = 0; t < nt; t++) {
+    pthread_join(th[t], NULL);
+    total += rj[t].out.cnt;
+  }
+  orc_factor *all = (orc_factor *)malloc((total ? total : 1) * sizeof(orc_factor));
+  size_t pos = 0;
+  for (int t = 0; t < nt; t++) {
+    for (size_t i = 0; i < rj[t].out.cnt; i++) all[pos++] = rj[t].out.v[i];
+    free(rj[t].out.v);
+  }
+  qsort(all, total, sizeof(orc_factor), cmp_factor);
+  for (size_t i = 0; i < total && i < cap; i++) out[i] = all[i];
+  *count = total;
+  free(all);
+  free(rj);
+  free(th);
+  free(cand);
+  free(row_ki);
+  return 0;
+}

@@ -14,6 +14,10 @@
  *   - the sieve contract itself          kernel_v0.24.6.cu:273-684
  *     (p | k*b^n-1  <=>  k*b^n == 1 mod p), restated as a textbook
  *     baby-step/giant-step search that is structurally unlike the GPU kernel.
+ *   - the reference run's observable output (reference projection):
+ *     its probable primes, one report per prime, Q=1 fallback, x-window
+ *     and host filter                    kernel_v0.24.6.cu:288-620,1605-1732,
+ *                                        1271-1303,1838-1987
  *
  * Parity pins (tests/test_oracle.py): the structural facts of the reference's
  * own test file sr_745.abcd (Q=18, 198 rows, x-range 3743, tMin=19, tMax=28
@@ -80,6 +84,19 @@ size_t orc_primes(uint64_t lo, uint64_t hi, uint64_t *out, size_t cap);
  * exceed cap (only cap written).  nthreads <= 0 means all cores. */
 int orc_sieve(const orc_job *job, uint64_t p0, uint64_t p1, int32_t datless, int32_t nthreads,
               orc_factor *out, size_t cap, size_t *count, uint64_t *nprimes);
+
+/* Reference projection: the factor lines one run of the reference executable
+ * would write for [p0, p1] with its plan pl (orc_ref_plan with the same
+ * hash_elems = 2<<M for -m M), -s small_prime_scale and verify (1, or 0 for
+ * -v): at most one (k, n) per candidate q, q from its probable-prime source
+ * (odd numbers free of the first 4096*s odd primes, composites included above
+ * that bound), chosen and filtered as kernel_v0.24.6.cu:288-620 and
+ * 1605-1732 do.  Riesel jobs only, p0 > b and p0 > every k.  Sorted by
+ * (p, k, n); *ncand = candidates q tested.  Returns 0, or 1 for arguments
+ * outside that domain. */
+int orc_sieve_ref(const orc_job *job, const orc_refplan *pl, int32_t hash_elems, int32_t small_prime_scale,
+                  uint64_t p0, uint64_t p1, int32_t verify, int32_t nthreads, orc_factor *out, size_t cap,
+                  size_t *count, uint64_t *ncand);
 
 /* Direct check p | k*b^n+sign by square-and-multiply (kernel_v0.24.6.cu:1649-1671). */
 int orc_verify(uint64_t p, uint32_t k, uint32_t b, uint32_t n, int32_t sign);

@@ -397,3 +397,35 @@ def test_per_sequence_bases(rs, oracle_mod, datless):
     assert st["primes"] == npr
     assert got == sorted(want)
     assert len({(b, c) for *_, b, c in got}) == 3 if datless else len(got) >= 5
+
+
+@pytest.mark.parametrize("window", ["sr745_default", "plain_1e9", "plain_2_33"])
+def test_contains_reference_projection(rs, oracle_mod, sr745_text, kat, window):
+    """Every factor line the reference executable would write (the oracle's
+    reference projection: its probable primes, one report per prime, its Q=1
+    fallback and x-window, kernel_v0.24.6.cu:288-620,1605-1732) is in the GPU's
+    complete set on the same input and range, with and without -v."""
+    import rsieve.synth as S
+
+    if window == "sr745_default":
+        text = sr745_text
+        p0 = kat["default_range"]["low"]
+        p1 = p0 + kat["default_range"]["width_per_scale"]
+    else:
+        b, s, ks, nl = S.plain_job(1)
+        text = S.to_abcd(b, s, ks, nl)
+        p0 = 10**9 if window == "plain_1e9" else _NEAR_2_33
+        p1 = p0 + 2 * 10**6
+    oj = oracle_mod.Job.from_abcd(text)
+    for verify in (True, False):
+        ref, _ = oj.sieve_ref(p0, p1, Qin=18, hash_m=8, verify=verify)
+        with rs.Job(text, datless=int(not verify)) as job:
+            g, st = job.sieve(p0, p1)
+        got = set(_set(g))
+        want = set(_set(ref))
+        assert want <= got, sorted(want - got)[:5]
+        if window == "sr745_default" and not verify:
+            d = kat["datless"]
+            assert (d["p"], d["k"], d["n"]) in want
+        if window != "sr745_default":
+            assert len(want) > 0

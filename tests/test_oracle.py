@@ -124,3 +124,60 @@ def test_oracle_abcd_errors(oracle_mod):
         oracle_mod.Job.from_abcd("ABCD 3*2^$a-1 [10]\n-5\n")
     with pytest.raises(ValueError):
         oracle_mod.Job.from_abcd("ABCD 3*2^$a-1 [10]\nABCD 5*3^$a-1 [10]\n")
+
+
+# --- reference projection: what one run of the reference executable writes ---
+
+def _trip(f):
+    return {(int(x["p"]), int(x["k"]), int(x["n"])) for x in f}
+
+
+def test_projection_reproduces_datless_kat(oracle_mod, sr745_text, kat):
+    """On the reference's own file and default range with -Q 18 -m 8 -v, the
+    projection writes exactly the debug prime's factor of kernel_v0.24.6.cu:244;
+    with verification on it writes nothing (n = 242670 is not a candidate)."""
+    d = kat["datless"]
+    lo = kat["default_range"]["low"]
+    hi = lo + kat["default_range"]["width_per_scale"]
+    job = oracle_mod.Job.from_abcd(sr745_text)
+    f, ncand = job.sieve_ref(lo, hi, Qin=18, hash_m=8, verify=False)
+    assert _trip(f) == {(d["p"], d["k"], d["n"])}
+    f, _ = job.sieve_ref(lo, hi, Qin=18, hash_m=8, verify=True)
+    assert len(f) == 0
+    # below smallP_max^2 (s = 256) the reference's probable primes are the primes
+    _, npr = job.sieve(lo, hi, datless=True)
+    assert ncand == npr
+
+
+def test_projection_is_subset_of_complete_set(oracle_mod):
+    """On dense synthetic data the reference falls back to Q=1 and writes at
+    most one factor per prime: its output is a strict subset of the complete
+    set (verified and datless), as stated in the contract differences."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    job = oracle_mod.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    p0, p1 = 10**9, 10**9 + 2 * 10**6
+    for verify in (True, False):
+        ref, ncand = job.sieve_ref(p0, p1, Qin=18, hash_m=8, verify=verify)
+        full, npr = job.sieve(p0, p1, datless=not verify)
+        assert ncand == npr
+        r, c = _trip(ref), _trip(full)
+        assert r <= c and len(r) < len(c)
+        assert len({p for p, _, _ in r}) == len(r)  # one report per prime
+        assert len(r) >= 5
+
+
+def test_projection_sends_composites_above_small_prime_bound(oracle_mod):
+    """With -s 1 the reference's probable-prime source keeps composites above
+    (the 4096th odd prime)^2 ~ 1.5e9; every line it writes still divides."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    job = oracle_mod.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    p0, p1 = 5 * 10**9, 5 * 10**9 + 2 * 10**6
+    ref, ncand = job.sieve_ref(p0, p1, Qin=0, hash_m=8, small_prime_scale=1, verify=False)
+    npr = len(oracle_mod.primes(p0, p1))
+    assert ncand > npr
+    for p, k, n in _trip(ref):
+        assert oracle_mod.verify(p, k, b, n, -1)
