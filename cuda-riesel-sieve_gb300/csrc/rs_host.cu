@@ -707,6 +707,7 @@ static uint32_t plan_row_form(const Plan &pl, const Seqs &s, std::vector<uint32_
     else if (row_c) (*row_c)[r] = (uint32_t)c;
   }
   if (!ints) return kRowsV;
+  if (!pl.cta && pl.nrows <= kMaskRows) return kRowsMask;
   const uint32_t vslots = (std::max<uint32_t>(1, pl.nrows) + 1) & ~1u;
   const uint32_t el_v = pl.cta ? kElWoff + 2 * kCtaWarps : kElV;
   const bool ids = pl.cta ? pl.steps_per_lane >= 2 : (el_v + vslots) * 8 > 2048;
@@ -844,13 +845,19 @@ static int upload_part(rs_job *j, Part &pt) {
   d.max_act = std::max<uint32_t>(1, pl.nrows);
   d.int_rows = form != kRowsV ? 1u : 0u;
   d.row_ids_only = form == kRowsIntId ? 1u : 0u;  // no V in the record
+  d.row_mask = form == kRowsMask ? 1u : 0u;       // neither V nor row ids: an active-row mask
   d.el_v = d.cta_warps > 1 ? kElWoff + 2 * d.cta_warps : kElV;
-  d.el_row = d.el_v + (d.row_ids_only ? 0u : ((d.max_act + 1) & ~1u));  // even: row ids are written 16 bytes at a time
-  d.el_tab = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
+  if (d.row_mask) {
+    d.el_row = d.el_v;
+    d.el_tab = d.el_v + 2;
+  } else {
+    d.el_row = d.el_v + (d.row_ids_only ? 0u : ((d.max_act + 1) & ~1u));  // even: row ids are written 16 bytes at a time
+    d.el_tab = d.el_row + 2 * ((d.max_act + 7) / 8);  // even, row ids in 16-byte groups
+  }
   d.rec_elems = d.el_tab + 64;
   // the warp kernel's staged part of a record: header + V (header + row ids
-  // without V) when it fits 2 KB; else the header alone
-  const uint32_t staged = d.row_ids_only ? d.el_tab : d.el_row;
+  // without V, header + mask with row_mask) when it fits 2 KB; else the header alone
+  const uint32_t staged = d.row_ids_only || d.row_mask ? d.el_tab : d.el_row;
   if (staged * 8 <= 2048) {
     d.stage_full = 1;
     d.stage_elems = staged;
@@ -860,8 +867,10 @@ static int upload_part(rs_job *j, Part &pt) {
   }
   if (d.cta_warps > 1)  // bytes per CTA: table, counts, V, match list
     d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 8 * ((d.max_act + 1) & ~1u) + kCtaMatchCap * 16 + 16, 16);
-  else  // bytes per warp: table, counts, two record stages, match list
-    d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + kMatchCap * 16 + 16, 16);
+  else  // bytes per warp: table, counts, two record stages, (V of a row mask,) match list
+    d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + (d.row_mask ? 8 * kMaskRows : 0) +
+                                         kMatchCap * 16 + 16,
+                                     16);
   d.row_r = (const uint32_t *)(b + o_rr);
   d.row_kidx = (const uint32_t *)(b + o_rk);
   d.row_c = (const uint32_t *)(b + o_rc);

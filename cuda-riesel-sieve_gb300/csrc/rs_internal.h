@@ -51,15 +51,21 @@ constexpr uint32_t kNoTable = 0xffffffffu;  // no quadratic-character table for 
 // the giant value, as V*G^s is in the general layout.  With row_ids_only the
 // record has no V at all (el_row == el_v) and the kernels read c from row_c by
 // the row id; this halves the setup kernel's scattered stores for jobs whose V
-// would not be staged whole anyway.
+// would not be staged whole anyway.  With row_mask (integer rows, a warp per
+// prime, at most 64 rows) the record keeps neither V nor row ids but one 64-bit
+// mask of the active rows at el_v (el_v+1 spare, el_tab = el_v + 2); the warp
+// kernel expands it into V (the integers c of the set bits, in row order) in
+// shared memory from row constants its lanes hold in registers.
 constexpr uint32_t kElP = 0, kElPinv = 1, kElBm = 2, kElGs = 3, kElNact = 4, kElRcp = 5;
 constexpr uint32_t kElStw = 6, kElStq = 7, kElOfw = 8, kElOfq = 9, kElGw = 10, kElGq = 11;
 constexpr uint32_t kElWoff = 12;   // warp offsets (W > 1)
 constexpr uint32_t kElV = 12;      // V in the warp-per-prime layout (W == 1)
 constexpr uint32_t kStepShoup = 0, kStepSmall = 1, kStepHigh = 2;  // ChunkBufs::small_step
 // Giant-step start values of the fast kernels (template argument): V in
-// Montgomery form, the integers k*b^r in V, or k*b^r read by row id.
-constexpr int kRowsV = 0, kRowsIntV = 1, kRowsIntId = 2;
+// Montgomery form, the integers k*b^r in V, k*b^r read by row id, or k*b^r of
+// the rows of an active-row mask.
+constexpr int kRowsV = 0, kRowsIntV = 1, kRowsIntId = 2, kRowsMask = 3;
+constexpr uint32_t kMaskRows = 64;  // rows a row_mask record can describe
 constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
 constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
@@ -84,6 +90,7 @@ struct JobDev {
   uint32_t pairable;     // Q == 2, a warp per prime and every k has rows for both residues
   uint32_t int_rows;     // every row's k*b^r < 2^32: V holds these integers (see the record layout)
   uint32_t row_ids_only; // integer rows whose records keep no V: the kernels read k*b^r by row id
+  uint32_t row_mask;     // integer rows whose records keep only a mask of the active rows (see above)
   uint32_t T;            // giant steps per row
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes

@@ -345,9 +345,16 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
   const bool qeven = (J.Q & 1u) == 0;
   uint32_t nact = 0;
   uint64_t vprev = 0, rp0 = 0, rp1 = 0;
+  uint64_t rows_on = 0;  // row_mask: the active rows as bits
   // one active row: its start value V and its row id, packed into the record
-  // (integer rows: the row id only, the kernels look up k*b^r by it)
+  // (integer rows: the row id only, the kernels look up k*b^r by it; row_mask:
+  // one bit)
   auto emit = [&](uint64_t V, uint32_t row) {
+    if (J.row_mask) {
+      rows_on |= 1ull << row;
+      nact++;
+      return;
+    }
     if (nact & 1) {
       if (live && !J.row_ids_only) rec_st2(rec, J.el_v + nact - 1, vprev, V);
     } else {
@@ -402,7 +409,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           const uint32_t r = __ffs(amask) - 1;
           amask &= amask - 1;
           const uint32_t row = ki.row0 + __popc(ki.rmask & ((1u << r) - 1));
-          emit(J.int_rows ? (J.row_ids_only ? 0 : (uint64_t)__ldg(J.row_c + row))
+          emit(J.int_rows ? (J.row_ids_only || J.row_mask ? 0 : (uint64_t)__ldg(J.row_c + row))
                           : shoup_mul(kx, S.hb[r][0][lane], S.hb[r][1][lane], p),
                row);
         }
@@ -437,7 +444,7 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
           const bool act = qeven ? (chik * ((r & 1u) ? chib : 1) == 1) : (chib == -1 || chik == 1);
           if (!act) continue;
           if (J.int_rows) {
-            emit(J.row_ids_only ? 0 : (uint64_t)__ldg(J.row_c + row), row);
+            emit(J.row_ids_only || J.row_mask ? 0 : (uint64_t)__ldg(J.row_c + row), row);
             continue;
           }
           if (!have) {
@@ -452,8 +459,12 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
     }
   }
   if (!live) return;
-  if ((nact & 1) && !J.row_ids_only) rec[J.el_v + nact - 1] = vprev;
-  if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
+  if (J.row_mask) {
+    rec_st2(rec, J.el_v, rows_on, 0);
+  } else {
+    if ((nact & 1) && !J.row_ids_only) rec[J.el_v + nact - 1] = vprev;
+    if (nact & 7) rec_st2(rec, J.el_row + ((nact >> 3) << 1), rp0, rp1);
+  }
   rec_st2(rec, kElP, p, M.pinv);
   rec_st2(rec, kElBm, B, Gs);
   // floor(2^64/p) is the Shoup constant of 1, whose Montgomery form is `one`
@@ -555,6 +566,13 @@ __device__ __forceinline__ void stage_copy(uint64_t *dst, const JobDev &J, const
 __device__ __forceinline__ void stage_commit_empty() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Index of the n-th (from 0) set bit of a row mask (row_mask records).
+__device__ __forceinline__ uint32_t nth_row(uint64_t mask, uint32_t n) {
+#pragma unroll 1
+  for (uint32_t t = 0; t < n; t++) mask &= mask - 1;
+  return (uint32_t)(__ffsll((long long)mask) - 1);
+}
 
 struct __align__(16) Match {
   uint64_t y;     // giant-step value whose tag matched
@@ -771,9 +789,14 @@ __device__ __forceinline__ void giant_home_int(const WarpTable &W, const uint16_
 }
 
 // Per-warp shared memory of the fast kernel:
-//   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B][kMatchCap matches][count, 16 B]
+//   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B]
+//   ([kMaskRows V x 8 B], row_mask only)[kMatchCap matches][count, 16 B]
 // The stages hold a record's header and V (double-buffered with cp.async); each
 // lane's B^lane and G^(lane+1) entries are loaded into registers one prime ahead.
+// With row_mask the stage holds the header and the active-row mask, and the
+// warp writes V (the integers k*b^r of the active rows, in row order) into its
+// own buffer from the constants of rows lane and lane + 32 that each lane keeps
+// in registers.
 //
 // Each lane runs two independent product chains in both phases (baby steps
 // j = lane + 64t and j = lane + 32 + 64t; giant steps on two row slots at a
@@ -794,8 +817,9 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
   W.bmask = NB - 1;
   uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
+  uint64_t *vbuf = stage0 + 2 * J.stage_elems;  // row_mask: V of the current prime
   MatchList ML;
-  ML.list = reinterpret_cast<Match *>(stage0 + 2 * J.stage_elems);
+  ML.list = reinterpret_cast<Match *>(vbuf + (RM == kRowsMask ? kMaskRows : 0));
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
   ML.cap = kMatchCap;
   const uint32_t lane_t = lane & (TL - 1);
@@ -809,6 +833,11 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 
   uint64_t nBl = 0, nGl = 0;
   uint32_t npaired = 0;  // primes of this warp that took the row-pair path
+  uint32_t c_lo = 0, c_hi = 0;  // row_mask: k*b^r of rows lane and lane + 32
+  if constexpr (RM == kRowsMask) {
+    c_lo = lane < J.nrows ? __ldg(J.row_c + lane) : 0u;
+    c_hi = lane + 32 < J.nrows ? __ldg(J.row_c + lane + 32) : 0u;
+  }
   if (first < n) {
     stage_copy(stage0, J, cb, first, J.stage_elems, lane);
     nBl = __ldg(ltab + (size_t)first * J.rec_elems);
@@ -835,6 +864,12 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     __syncwarp();
     const uint32_t nact = (uint32_t)cur[kElNact];
     if (nact != 0) {
+      if constexpr (RM == kRowsMask) {  // V from the active-row mask
+        const uint64_t am = cur[kElV];
+        const uint32_t lo = (uint32_t)am, hi = (uint32_t)(am >> 32), below = (1u << lane) - 1u;
+        if ((lo >> lane) & 1u) vbuf[__popc(lo & below)] = c_lo;
+        if ((hi >> lane) & 1u) vbuf[__popc(lo) + __popc(hi & below)] = c_hi;
+      }
       const uint64_t p = cur[kElP], pinv = cur[kElPinv];
       // Multipliers in normal form with their Shoup constants; the values
       // they multiply stay in Montgomery form, so products stay comparable.
@@ -900,6 +935,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
       auto giant_val = [&](uint32_t sl) -> uint64_t {
         if constexpr (RM == kRowsIntId) return shoup_mul32(__ldg(J.row_c + Rs[sl]), Glw, Glq, p);
         else if constexpr (RM == kRowsIntV) return shoup_mul32((uint32_t)Vs[sl], Glw, Glq, p);
+        else if constexpr (RM == kRowsMask) return shoup_mul32((uint32_t)vbuf[sl], Glw, Glq, p);
         else return shoup_mul(Vs[sl], Glw, Glq, p);
       };
       if (spl == 1 && ngi <= 64) {
@@ -921,12 +957,13 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
           else
             giant_home_int<RPI>(W, Rs, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         } else {
-          constexpr bool INT = RM == kRowsIntV;
+          constexpr bool INT = RM == kRowsIntV || RM == kRowsMask;
+          const uint64_t *Vst = RM == kRowsMask ? vbuf : cur + kElV;  // V in shared memory
           if (paired && J.stage_full)
-            giant_home<RPI, RPI == 1, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+            giant_home<RPI, RPI == 1, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
                                            (uint32_t)cur[kElRcp]);
           else if (J.stage_full)
-            giant_home<RPI, false, INT>(W, cur + kElV, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+            giant_home<RPI, false, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
           else
             giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
         }
@@ -985,9 +1022,14 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
               for (uint32_t q = 0; q < mc; q++) {
                 const Match mt = ML.list[q];
                 if (mt.y == v) {
-                  const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
-                  record_hit(J, hb, p, (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu, mt.s,
-                             (h ? jb0 : ja0) + t);
+                  uint32_t row;
+                  if constexpr (RM == kRowsMask) {
+                    row = nth_row(cur[kElV], mt.slot);
+                  } else {
+                    const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                    row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
+                  }
+                  record_hit(J, hb, p, row, mt.s, (h ? jb0 : ja0) + t);
                 }
               }
             }
@@ -1018,11 +1060,12 @@ static BsgsFn bsgs_fn_t(uint32_t tlanes) {
 }
 
 static int row_mode(const JobDev &job) {
-  return job.row_ids_only ? kRowsIntId : job.int_rows ? kRowsIntV : kRowsV;
+  return job.row_mask ? kRowsMask : job.row_ids_only ? kRowsIntId : job.int_rows ? kRowsIntV : kRowsV;
 }
 
 static BsgsFn bsgs_fn(const JobDev &job) {
   switch (row_mode(job)) {
+    case kRowsMask: return bsgs_fn_t<kRowsMask>(job.tlanes);
     case kRowsIntId: return bsgs_fn_t<kRowsIntId>(job.tlanes);
     case kRowsIntV: return bsgs_fn_t<kRowsIntV>(job.tlanes);
     default: return bsgs_fn_t<kRowsV>(job.tlanes);
@@ -1302,10 +1345,13 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     for (uint32_t gi = 0; gi < ngi; gi++) {
       const uint32_t slot = gi * rows_pass + wig * J.rows_per_it + lane_row;
       if (slot < nact) {
-        const uint32_t row = (uint32_t)(rec_el(J, cb, J.el_row + (slot >> 2), i) >> (16 * (slot & 3))) & 0xffffu;
+        const uint32_t row = J.row_mask ? nth_row(rec_el(J, cb, J.el_v, i), slot)
+                                        : (uint32_t)(rec_el(J, cb, J.el_row + (slot >> 2), i) >> (16 * (slot & 3))) &
+                                              0xffffu;
         // integer rows: montmul(k*b^r, Z * 2^128) is the Montgomery form of the giant value
-        uint64_t y =
-            montmul(J.row_ids_only ? (uint64_t)__ldg(J.row_c + row) : rec_el(J, cb, J.el_v + slot, i), Gl, p, pinv);
+        uint64_t y = montmul(J.row_ids_only || J.row_mask ? (uint64_t)__ldg(J.row_c + row)
+                                                          : rec_el(J, cb, J.el_v + slot, i),
+                             Gl, p, pinv);
         uint32_t s = lane_t + 1;
 #pragma unroll 1
         for (uint32_t u = 0; u < J.steps_per_lane; u++) {

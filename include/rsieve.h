@@ -102,7 +102,9 @@ typedef struct {
   uint64_t upload_bytes; /* host->device bytes copied when the job was created */
   uint32_t warps_per_prime; /* 1: a warp per prime; 16: a CTA per prime (large tables) */
   uint32_t row_form;     /* giant-step start values: 0 per-prime residues, 1 the integers
-                            k*b^r (all < 2^32) in the records, 2 k*b^r read by row id */
+                            k*b^r (all < 2^32) in the records, 2 k*b^r read by row id,
+                            3 k*b^r of the rows of a per-prime active-row mask (at most
+                            64 rows, a warp per prime) */
   uint32_t parts;        /* (base, sign) groups of the input, each planned and searched as
                             its own part over the same primes; the plan fields above
                             describe the first part, num_k and num_candidates count all */

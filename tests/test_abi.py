@@ -234,13 +234,17 @@ def test_plan_layouts(rs):
 
 
 def test_plan_row_forms(rs, sr745_text):
-    """Giant-step start values: integers k*b^r in the records for the plain job
-    (k*745 < 2^32, a staged record), read by row id for the wide job (two giant
-    steps per lane on the CTA kernel), per-prime residues for sr_745.abcd
-    (Q = 18, so b^r is far above 2^32)."""
+    """Giant-step start values: an active-row mask for the plain job (44 rows,
+    every k*745 < 2^32, a warp per prime), the integers k*b^r in the records
+    for a warp-per-prime job with more than 64 rows, read by row id for the wide
+    job (two giant steps per lane on the CTA kernel), per-prime residues for
+    sr_745.abcd (Q = 18, so b^r is far above 2^32)."""
     import rsieve.synth as S
 
-    assert rs.plan_abcd(S.to_abcd(*S.plain_job(1)))["row_form"] == 1
+    assert rs.plan_abcd(S.to_abcd(*S.plain_job(1)))["row_form"] == 3
+    (b, s, ks, nl), _ = S.batch_job(7, 48)
+    d = rs.plan_abcd(S.to_abcd(b, s, ks, nl), datless=1)
+    assert (d["row_form"], d["warps_per_prime"]) == (1, 1) and d["rows"] > 64
     body = "\n".join(["1"] * 47 + [str(3 * 10**6 - 10**6 - 47)])
     wide = "".join(f"ABCD {k}*2^$a-1 [1000000]\n{body}\n" for k in range(3, 2003, 2))
     d = rs.plan_abcd(wide)

@@ -119,7 +119,7 @@ def test_benchmark_path_near_2_33(rs, oracle_mod, sign, datless, width):
     b, _, ks, nl = S.plain_job(1)
     g, o, st = _both(rs, oracle_mod, b, sign, ks, nl, _NEAR_2_33, _NEAR_2_33 + width - 1, datless=datless)
     info = st["info"]
-    assert (info["Q"], info["warps_per_prime"], info["row_form"]) == (2, 1, 1)
+    assert (info["Q"], info["warps_per_prime"], info["row_form"]) == (2, 1, 3)
     assert len(o) >= 5
     assert g == o
     assert st["primes_by_step"]["short"] == st["primes"]
@@ -284,13 +284,14 @@ def test_batch_shaped_jobs(rs, oracle_mod, i):
     assert g == o and st["primes"] > 1000
 
 
-@pytest.mark.parametrize("i,form,wpp", [(20, 1, 16), (5, 0, 16), (8, 2, 16), (4, 1, 1), (19, 1, 1), (62, 2, 1)])
+@pytest.mark.parametrize("i,form,wpp", [(20, 1, 16), (5, 0, 16), (8, 2, 16), (4, 3, 1), (19, 3, 1), (48, 1, 1),
+                                        (62, 2, 1)])
 def test_row_forms(rs, oracle_mod, i, form, wpp):
     """Each form of the giant-step start values on each kernel: per-prime
-    residues (form 0), the integers k*b^r kept in the records (form 1) and
-    k*b^r read by row id (form 2), with a warp (wpp 1) or a CTA (16) per
-    prime, on mixed-batch jobs at small p (with factors) and in their own
-    window near 2^60."""
+    residues (form 0), the integers k*b^r kept in the records (form 1),
+    k*b^r read by row id (form 2) and an active-row mask (form 3), with a warp
+    (wpp 1) or a CTA (16) per prime, on mixed-batch jobs at small p (with
+    factors), just above 2^33 and in their own window near 2^60."""
     import rsieve.synth as S
 
     (b, s, ks, nl), (p0, _) = S.batch_job(7, i)
