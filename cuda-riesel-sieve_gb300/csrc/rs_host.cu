@@ -626,7 +626,8 @@ struct Part {
   Plan plan;
   JobDev dev{};
   void *d_job = nullptr;  // job arrays
-  size_t job_bytes = 0;
+  size_t job_bytes = 0;   // bytes uploaded into them
+  size_t dev_bytes = 0;   // their device size (with the character tables built on the device)
   HitBufs hb{};
   void *d_hits = nullptr;
   int bsgs_grid = 0;
@@ -712,6 +713,38 @@ static uint32_t plan_row_form(const Plan &pl, const Seqs &s, std::vector<uint32_
   const uint32_t el_v = pl.cta ? kElWoff + 2 * kCtaWarps : kElV;
   const bool ids = pl.cta ? pl.steps_per_lane >= 2 : (el_v + vslots) * 8 > 2048;
   return ids ? kRowsIntId : kRowsIntV;
+}
+
+// First element of the lane tables in a record (el_tab; a record has el_tab + 64
+// elements), from the plan and the row form, as upload_part lays it out.
+static uint32_t record_el_tab(const Plan &pl, uint32_t form) {
+  const uint32_t el_v = pl.cta ? kElWoff + 2 * kCtaWarps : kElV;
+  if (form == kRowsMask) return el_v + 2;
+  const uint32_t max_act = std::max<uint32_t>(1, pl.nrows);
+  const uint32_t el_row = el_v + (form == kRowsIntId ? 0u : ((max_act + 1) & ~1u));
+  return el_row + 2 * ((max_act + 7) / 8);
+}
+
+// Device bytes of a part's job arrays (upload_part's single allocation,
+// character tables included), from a plan made without the bitmap.
+static uint64_t part_array_bytes(const Plan &pl, const Seqs &s, bool datless) {
+  const uint64_t nk = s.k.size(), nr = pl.nrows;
+  uint64_t b = 3 * nr * 4 + nk * (4 + 4 + 4 + 8 + 4 + sizeof(KInfo)) + (nk + 1) * 4;
+  b += datless ? 4 : nr * (uint64_t)pl.words_per_row * 4;
+  std::vector<uint32_t> odd;
+  for (uint32_t k : s.k) {
+    while (!(k & 1)) k >>= 1;
+    if (k > 1) odd.push_back(k);
+  }
+  uint32_t bo = s.base;
+  while (!(bo & 1)) bo >>= 1;
+  if (bo > 1) odd.push_back(bo);
+  std::sort(odd.begin(), odd.end());
+  odd.erase(std::unique(odd.begin(), odd.end()), odd.end());
+  uint64_t words = 0;
+  for (uint32_t k : odd) words += (k + 31) / 32;
+  if (words <= (256ull << 20)) b += words * 4 + odd.size() * 8;
+  return b + 20 * 256;  // section alignment
 }
 
 static int upload_part(rs_job *j, Part &pt) {
@@ -804,6 +837,7 @@ static int upload_part(rs_job *j, Part &pt) {
   memcpy(host.data() + o_tk, tab_k.data(), tab_k.size() * 4);
   memcpy(host.data() + o_to, tab_off.data(), tab_off.size() * 4);
   CUDA_TRY(cudaMallocAsync(&pt.d_job, off, j->st));
+  pt.dev_bytes = off;
   CUDA_TRY(cudaMemcpyAsync(pt.d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
   uint8_t *b = (uint8_t *)pt.d_job;
   CUDA_TRY(launch_jacobi_tables((const uint32_t *)(b + o_tk), (const uint32_t *)(b + o_to),
@@ -1748,6 +1782,60 @@ extern "C" int rs_gpu_arith_check(const uint64_t *a, const uint64_t *b, const ui
   cudaFree(d);
   if (e != cudaSuccess) return fail(RS_ERR_CUDA, "arith check: %s", cudaGetErrorString(e));
   return RS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Helpers of the served form (rs_server.cu; declared in rs_internal.h).
+
+int rs::job_footprint(const char *text, size_t len, const rs_options &opt, JobFootprint *fp) {
+  Seqs all;
+  int rc = parse_abcd(text, len, all);
+  if (rc) return rc;
+  std::vector<Seqs> groups = split_parts(std::move(all));
+  *fp = JobFootprint{};
+  fp->parts = (uint32_t)groups.size();
+  uint32_t rec = 0;
+  for (Seqs &g : groups) {
+    normalise(g);
+    Plan pl;
+    rc = make_plan(g, opt, pl, false);
+    if (rc) return rc;
+    fp->arrays += part_array_bytes(pl, g, opt.datless != 0);
+    rec = std::max(rec, record_el_tab(pl, plan_row_form(pl, g, nullptr)) + 64);
+  }
+  fp->per_prime = 8 + 4 + 8 * (uint64_t)rec;
+  return RS_OK;
+}
+
+uint64_t rs::job_resident_bytes(const rs_job *j) {
+  uint64_t b = 0;
+  for (auto &pt : j->parts) b += pt->dev_bytes;
+  return b;
+}
+
+void rs::job_set_mem_limit(rs_job *j, uint64_t bytes) {
+  std::lock_guard<std::mutex> lock(j->mu);
+  j->opt.mem_limit = bytes;
+  j->opt.block_scale = j->opt.thread_scale = 0;
+  set_chunk_cap(j);
+}
+
+void rs::job_release_buffers(rs_job *j) {
+  std::lock_guard<std::mutex> lock(j->mu);
+  cudaSetDevice(j->device);
+  if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
+  j->d_chunk = nullptr;
+  j->chunk_cap = 0;
+  j->chunk_rec_elems = 0;
+  for (auto &pt : j->parts) {
+    if (pt->d_hits) cudaFreeAsync(pt->d_hits, j->st);
+    pt->d_hits = nullptr;
+    pt->hb = HitBufs{};
+  }
+  if (j->d_gbits) cudaFreeAsync(j->d_gbits, j->st);
+  j->d_gbits = nullptr;
+  j->gbits_words = 0;
+  cudaStreamSynchronize(j->st);
 }
 
 // ---------------------------------------------------------------------------

@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include "rsieve.h"
+
 namespace rs {
 
 // BSGS fast path: per-prime hash of 16-bit tags, kBucket tags per 16-byte bucket.
@@ -184,6 +186,20 @@ cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off,
                                  uint32_t total_words, uint32_t *bits, cudaStream_t st);
 // Record an error for rs_last_error() and return code (rs_host.cu).
 int set_error(int code, const char *fmt, ...);
+
+// Served-form helpers (rs_host.cu, used by rs_server.cu).
+// Device bytes a job from this ABCD text will hold, from a host-only plan:
+// its arrays (character tables included) and its chunk buffers per prime of
+// a launch (prime, count share and record).
+struct JobFootprint {
+  uint64_t arrays = 0;
+  uint64_t per_prime = 0;
+  uint32_t parts = 0;
+};
+int job_footprint(const char *text, size_t len, const rs_options &opt, JobFootprint *fp);
+uint64_t job_resident_bytes(const rs_job *j);          // device bytes of its arrays
+void job_set_mem_limit(rs_job *j, uint64_t bytes);     // chunk-buffer budget for later calls
+void job_release_buffers(rs_job *j);                   // free its per-launch buffers, keep its arrays
 
 cudaError_t run_imad_bench(int device, double *mul_ops_per_s, double *montmul_per_s, double *shoup_per_s);
 // rates[6]: mad.lo.u32 per second, then 64-bit modular products per second by

@@ -124,7 +124,7 @@ class ServerOptions(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("slots", ctypes.c_uint32),
         ("queue_cap", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("cache_jobs", ctypes.c_uint32),
         ("mem_budget", ctypes.c_uint64),
     ]
 
@@ -132,7 +132,7 @@ class ServerOptions(ctypes.Structure):
 class JobReport(ctypes.Structure):
     _fields_ = [
         ("status", ctypes.c_int32),
-        ("reserved", ctypes.c_uint32),
+        ("resident", ctypes.c_uint32),
         ("primes", ctypes.c_uint64),
         ("factors", ctypes.c_uint64),
         ("p_covered", ctypes.c_uint64),
@@ -140,10 +140,13 @@ class JobReport(ctypes.Structure):
         ("run_ms", ctypes.c_double),
         ("latency_ms", ctypes.c_double),
         ("gpu_ms", ctypes.c_double),
+        ("create_ms", ctypes.c_double),
+        ("mem_bytes", ctypes.c_uint64),
+        ("mem_in_use", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 _lib = None
@@ -286,7 +289,8 @@ class Job:
 class Server:
     """A job server on one GPU (rs_server_*): jobs run concurrently in `slots`."""
 
-    def __init__(self, device: int = 0, slots: int = 0, queue_cap: int = 0, mem_budget: int = 0):
+    def __init__(self, device: int = 0, slots: int = 0, queue_cap: int = 0, mem_budget: int = 0,
+                 cache_jobs: int = 0):
         self._h = ctypes.c_void_p(None)
         o = ServerOptions()
         lib().rs_server_options_default(ctypes.byref(o))
@@ -297,6 +301,8 @@ class Server:
             o.queue_cap = queue_cap
         if mem_budget:
             o.mem_budget = mem_budget
+        if cache_jobs:
+            o.cache_jobs = cache_jobs
         _check(lib().rs_server_create(ctypes.byref(o), ctypes.byref(self._h)))
 
     def submit(self, abcd: str | bytes, p0: int, p1: int, **opts) -> int:

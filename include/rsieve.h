@@ -264,13 +264,18 @@ const char *rs_version(void);
 
 /* ------------------------------------------------------------------------
  * Serving (no counterpart in the reference, which runs one job per process).
- * A server owns a device and runs submitted jobs concurrently: each of
- * `slots` worker threads admits the oldest waiting job when it is free, creates
- * it, sieves its range on its own stream and releases it, so jobs that arrive
- * while others run overlap on the GPU.  Device memory is partitioned: every
- * running job's per-launch buffers are limited to mem_budget / slots.  Results
- * are identical to running each job alone through rs_job_create_abcd +
- * rs_sieve_range (the same kernels on the same inputs).
+ * A server owns a device and runs submitted jobs concurrently on `slots`
+ * worker threads.  Admission is by device memory: at submit a job's footprint
+ * is computed on the host (its arrays plus per-launch buffers sized for its
+ * p-window), and the oldest waiting job starts when a slot is free and its
+ * footprint fits mem_budget next to the running jobs (a job larger than the
+ * budget runs when no other does).  Finished jobs keep their arrays resident
+ * (rows, per-k data, candidate bitmaps, character tables): a later request
+ * with the same ABCD text and options takes them over and skips parsing,
+ * planning and upload.  Idle resident jobs count against the budget and are
+ * evicted least recently used first.  Results are identical to running each
+ * job alone through rs_job_create_abcd + rs_sieve_range (the same kernels on
+ * the same inputs).
  * ------------------------------------------------------------------------ */
 typedef struct rs_server rs_server;
 
@@ -278,28 +283,33 @@ typedef struct {
   int32_t device;       /* CUDA device ordinal */
   uint32_t slots;       /* jobs running at once; 0 = 4 */
   uint32_t queue_cap;   /* jobs waiting for a slot before submit returns RS_ERR_BUSY; 0 = 1024 */
-  uint32_t reserved;    /* 0 */
-  uint64_t mem_budget;  /* device bytes shared by the running jobs; 0 = 64 GiB */
+  uint32_t cache_jobs;  /* idle jobs kept resident at most; 0 = 64 */
+  uint64_t mem_budget;  /* device bytes for running and resident jobs; 0 = 64 GiB */
 } rs_server_options;
 
 /* Timing and counters of one served job (host clock unless noted). */
 typedef struct {
   int32_t status;       /* the job's rs_* status */
-  uint32_t reserved;
+  uint32_t resident;    /* 1 if it ran on the resident arrays of an earlier request */
   uint64_t primes;      /* primes sieved */
   uint64_t factors;     /* factors found */
   uint64_t p_covered;   /* width of the p-interval covered */
   double queue_ms;      /* submit -> admitted to a slot */
-  double run_ms;        /* admitted -> finished (job creation, sieve, release) */
+  double run_ms;        /* admitted -> finished (job creation unless resident, sieve, release) */
   double latency_ms;    /* submit -> finished */
   double gpu_ms;        /* CUDA-event time of the job's kernels */
+  double create_ms;     /* parse, plan and upload (0 when resident) */
+  uint64_t mem_bytes;   /* device bytes charged to the job while it ran */
+  uint64_t mem_in_use;  /* bytes charged to all running jobs just after its admission */
 } rs_job_report;
 
 void rs_server_options_default(rs_server_options *opt);
 int rs_server_create(const rs_server_options *opt, rs_server **server);
-/* Queue a job: the ABCD text (copied), its options (mem_limit is set by the
- * server) and the range [p0, p1].  *ticket identifies it to rs_server_wait.
- * RS_ERR_BUSY when queue_cap jobs are already waiting. */
+/* Queue a job: the ABCD text (copied), its options (mem_limit, -b and -t are
+ * set by the server) and the range [p0, p1].  The text is parsed and planned
+ * here, unless the same job was submitted before, so a malformed job fails at
+ * submit.  *ticket identifies it to rs_server_wait.  RS_ERR_BUSY when
+ * queue_cap jobs are already waiting. */
 int rs_server_submit(rs_server *server, const char *abcd, size_t len, const rs_options *opt, uint64_t p0,
                      uint64_t p1, uint64_t *ticket);
 /* Wait up to timeout_ms (< 0: no limit) for a job.  RS_ERR_TIMEOUT if it has
