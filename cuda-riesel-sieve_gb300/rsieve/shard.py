@@ -28,9 +28,11 @@ def shard_range(p0: int, p1: int, rank: int, world: int) -> tuple[int, int]:
 
 
 def merge(parts) -> np.ndarray:
-    """Concatenate per-rank factor arrays (fields p, k, n) sorted by (p, k, n)."""
+    """Concatenate per-rank factor arrays (fields p, k, n, and b, c when present)
+    sorted by (p, k, n, b, c), the order rs_sieve_range returns."""
     parts = [np.asarray(x) for x in parts if len(x)]
     if not parts:
         return np.zeros(0, dtype=[("p", "<u8"), ("k", "<u4"), ("n", "<u4")])
     allf = np.concatenate(parts)
-    return allf[np.lexsort((allf["n"], allf["k"], allf["p"]))]
+    keys = [allf[f] for f in ("c", "b") if f in allf.dtype.names] + [allf["n"], allf["k"], allf["p"]]
+    return allf[np.lexsort(keys)]
