@@ -344,6 +344,7 @@ static void normalise(Seqs &s) {
 struct Plan {
   uint32_t Q = 0, nrows = 0, X = 0, x_lo = 0, x_hi = 0, m = 0, T = 0;
   uint32_t tlanes = 0, rows_per_it = 0, steps_per_lane = 0, table_log2 = 0, jbits = 0, bucket_log2 = 0;
+  uint32_t nbuckets = 0;  // fast-path buckets (1 << bucket_log2 for the warp kernel; a multiple of 64 for a CTA)
   bool cta = false;  // one CTA of kCtaWarps warps per prime (bsgs_cta_kernel)
   uint32_t nmin = 0, nmax = 0, ncand = 0, words_per_row = 0;
   int64_t e0 = 0;
@@ -385,6 +386,7 @@ struct PlanChoice {
   uint32_t Q = 0, T = 0, m = 0;
   bool cta = false;
   double cost = 0;
+  uint32_t nb = 0;  // fast-path buckets
 };
 
 // Plan a job.  With `force`, take exactly that choice (it must be feasible);
@@ -429,10 +431,19 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
     const uint32_t X = nmax / Q - nmin / Q + 1;
     const int rows = count_rows(s, Q, datless);
     const double ER = rows * ((Q & 1) ? 0.75 : 0.5);
-    auto consider = [&](bool cta, uint64_t T, uint64_t m, uint32_t blog, uint32_t slog, double cost) {
-      if (ranked) ranked->push_back(PlanChoice{Q, (uint32_t)T, (uint32_t)m, cta, cost});
+    // every row's k*b^r below 2^32 (integer rows; see plan_row_form)
+    bool ints_q = true;
+    {
+      uint64_t kmax = 0;
+      for (uint32_t k : s.k) kmax = std::max<uint64_t>(kmax, k);
+      uint64_t c = kmax;
+      for (uint32_t e = 1; e < Q && c < (1ull << 32); e++) c *= s.base;
+      ints_q = c < (1ull << 32);
+    }
+    auto consider = [&](bool cta, uint64_t T, uint64_t m, uint32_t blog, uint32_t nb, uint32_t slog, double cost) {
+      if (ranked) ranked->push_back(PlanChoice{Q, (uint32_t)T, (uint32_t)m, cta, cost, nb});
       if (force) {
-        if (force->Q != Q || force->T != T || force->m != m || force->cta != cta) return;
+        if (force->Q != Q || force->T != T || force->m != m || force->cta != cta || force->nb != nb) return;
         cost = -1.0;  // the forced choice wins
       }
       if (cost < best) {
@@ -447,6 +458,7 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
         pl.steps_per_lane = (uint32_t)std::max<uint64_t>(1, T / 32);
         pl.table_log2 = slog;
         pl.bucket_log2 = blog;
+        pl.nbuckets = nb;
         pl.cta = cta;
         pl.cost = cost;
         pl.work_per_prime = 2.0 * std::sqrt(ER * (double)X);
@@ -481,23 +493,34 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
             const double cost = (std::ceil((double)m / 32.0) + kGiantWeight * std::ceil(ER / rpi) * spl +
                                  nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
                                 std::sqrt(kFullWarps / warps);
-            consider(false, T, m, blog, slog, cost);
+            consider(false, T, m, blog, 1u << blog, slog, cost);
           }
         }
       }
-      if (T >= 32 && T <= 256) {  // a CTA per prime: 64 * kCtaWarps chains share a table of up to ~160 KB
+      if (T >= 32 && T <= 256) {  // a CTA per prime: 64 * kCtaWarps chains share a table of up to ~220 KB
         const uint64_t chains = 64 * kCtaWarps;
         const uint64_t m = (m0 + chains - 1) / chains * chains;
+        // exact-path table (rare primes): shared memory up to 2^15 slots, else global scratch
         const uint32_t slog = std::max<uint32_t>(7, ilog2_ceil(2 * m));
-        const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((m + 1) / 2));  // <= 2 entries per bucket
-        const double nb = (double)(1u << blog);
-        const double smem = 20.0 * nb + 8.0 * (rows + 2) + 16.0 * (kCtaMatchCap + 1);
-        const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
-        if (m <= mcap && m * T >= X && slog <= 15 && smem <= 232448.0 && fp <= 16.0) {
-          const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
-                               nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
-                              std::sqrt(kFullWarps / kCtaWarps) * kCtaStepCost;
-          consider(true, T, m, blog, slog, cost);
+        // V staging: the integers k*b^r read by row id (two bytes a row) when a lane takes
+        // two or more giant steps, else eight bytes a row (the row form of plan_row_form)
+        const double vbytes = (ints_q && T >= 64 ? 2.0 : 8.0) * (rows + 2) + 16.0;
+        // buckets: a power of two with at most ~2 entries each, or any multiple of 64 with
+        // at most ~3 each (the table then fills the shared memory; overflow stays rare)
+        const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((m + 1) / 2));
+        const uint32_t nb_opts[2] = {1u << blog, (uint32_t)std::max<uint64_t>(64, ((m + 2) / 3 + 63) / 64 * 64)};
+        for (int o = 0; o < 2; o++) {
+          const uint32_t nbk = nb_opts[o];
+          if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536)) continue;
+          const double nb = (double)nbk;
+          const double smem = 20.0 * nb + vbytes + 16.0 * (kCtaMatchCap + 1);
+          const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
+          if (m <= mcap && m * T >= X && slog <= 17 && smem <= 232448.0 && fp <= 16.0) {
+            const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
+                                 nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
+                                std::sqrt(kFullWarps / kCtaWarps) * kCtaStepCost;
+            consider(true, T, m, blog, nbk, slog, cost);
+          }
         }
       }
     }
@@ -656,6 +679,7 @@ struct rs_job {
   size_t h_counts_cap = 0;
   uint32_t chunk_cap = 0;
   uint32_t chunk_rec_elems = 0;  // record elements the chunk buffers were sized for
+  uint64_t chunk_exact_bytes = 0;  // exact-kernel scratch they hold
   uint32_t max_rec_elems() const {
     uint32_t r = 0;
     for (auto &pt : parts) r = std::max(r, pt->dev.rec_elems);
@@ -865,6 +889,7 @@ static int upload_part(rs_job *j, Part &pt) {
   d.rows_per_it = pl.rows_per_it;
   d.steps_per_lane = pl.steps_per_lane;
   d.table_log2 = pl.bucket_log2;
+  d.nbuckets = pl.nbuckets;
   d.exact_log2 = pl.table_log2;
   d.jbits = pl.jbits;
   d.nrows = pl.nrows;
@@ -899,8 +924,11 @@ static int upload_part(rs_job *j, Part &pt) {
     d.stage_full = 0;
     d.stage_elems = d.el_v;
   }
-  if (d.cta_warps > 1)  // bytes per CTA: table, counts, V, match list
-    d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 8 * ((d.max_act + 1) & ~1u) + kCtaMatchCap * 16 + 16, 16);
+  if (d.cta_warps > 1)  // bytes per CTA: table, counts, V (or row ids), match list
+    d.warp_smem = (uint32_t)align_up(20u * d.nbuckets +
+                                         (d.row_ids_only ? 16 * ((d.max_act + 7) / 8) : 8 * ((d.max_act + 1) & ~1u)) +
+                                         kCtaMatchCap * 16 + 16,
+                                     16);
   else  // bytes per warp: table, counts, two record stages, (V of a row mask,) match list
     d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + (d.row_mask ? 8 * kMaskRows : 0) +
                                          kMatchCap * 16 + 16,
@@ -988,9 +1016,16 @@ static int ensure_gbits(rs_job *j, uint64_t words) {
 
 static size_t chunk_bytes_per_prime(const rs_job *j) { return 8 + 4 + 8 * (size_t)j->max_rec_elems(); }
 
+static uint64_t exact_scratch_bytes(const rs_job *j) {
+  uint64_t b = 0;
+  for (auto &pt : j->parts) b = std::max(b, bsgs_exact_scratch_bytes(pt->dev, pt->exact_grid));
+  return b;
+}
+
 static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   const uint32_t rec = j->max_rec_elems();
-  if (j->d_chunk && j->chunk_cap >= cap && j->chunk_rec_elems >= rec) return RS_OK;
+  const uint64_t xs = exact_scratch_bytes(j);
+  if (j->d_chunk && j->chunk_cap >= cap && j->chunk_rec_elems >= rec && j->chunk_exact_bytes >= xs) return RS_OK;
   if (j->d_chunk) cudaFreeAsync(j->d_chunk, j->st);
   j->d_chunk = nullptr;
   size_t off = 0;
@@ -1000,7 +1035,7 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
     return o;
   };
   const size_t o_pr = sec((size_t)cap * 8), o_ct = sec(16), o_rec = sec((size_t)cap * 8 * rec);
-  const size_t o_rd = sec((size_t)cap * 4), o_rc = sec(16);
+  const size_t o_rd = sec((size_t)cap * 4), o_rc = sec(16), o_xt = sec(xs);
   CUDA_TRY(cudaMallocAsync(&j->d_chunk, off, j->st));
   uint8_t *b = (uint8_t *)j->d_chunk;
   j->cb.primes = (uint64_t *)(b + o_pr);
@@ -1008,9 +1043,11 @@ static int ensure_chunk_buffers(rs_job *j, uint32_t cap) {
   j->cb.recs = (uint64_t *)(b + o_rec);
   j->cb.redo = (uint32_t *)(b + o_rd);
   j->cb.redo_count = (uint32_t *)(b + o_rc);
+  j->cb.exact_tab = xs ? (uint32_t *)(b + o_xt) : nullptr;
   j->cb.cap = cap;
   j->chunk_cap = cap;
   j->chunk_rec_elems = rec;
+  j->chunk_exact_bytes = xs;
   return RS_OK;
 }
 
@@ -1082,6 +1119,12 @@ static void set_chunk_cap(rs_job *j) {
 // Upload and configure one planned part.
 static int make_part(rs_job *j, std::unique_ptr<Part> &pt) {
   int rc = upload_part(j, *pt);
+  if (!rc) {  // an exact-path table larger than the shared memory of a CTA lives in global scratch
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, j->device);
+    pt->dev.exact_global = 0;
+    pt->dev.exact_global = bsgs_exact_smem_bytes(pt->dev) > max_smem ? 1u : 0u;
+  }
   if (!rc) {
     const cudaError_t e = bsgs_configure(pt->dev, j->device, &pt->bsgs_grid, &pt->exact_grid);
     if (e != cudaSuccess) rc = fail(RS_ERR_CUDA, "bsgs_configure: %s", cudaGetErrorString(e));
@@ -1220,7 +1263,7 @@ int rs_job_info_get(const rs_job *j, rs_job_info *info) {
   info->x_range = pl.X;
   info->baby_steps = pl.m;
   info->giant_steps = pl.T;
-  info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
+  info->table_slots = (uint32_t)kBucket * pl.nbuckets;
   info->primes_per_launch = j->cb.cap;
   info->work_per_prime = pl.work_per_prime;
   info->warps_per_prime = pl.cta ? kCtaWarps : 1;
@@ -1560,7 +1603,7 @@ extern "C" int rs_job_autotune(rs_job *j, uint64_t p0, uint64_t p1, uint32_t can
     std::vector<PlanChoice> cand;
     for (const PlanChoice &c : cur.ranked) {
       bool dup = false;
-      for (const PlanChoice &d : cand) dup |= d.Q == c.Q && d.T == c.T && d.m == c.m && d.cta == c.cta;
+      for (const PlanChoice &d : cand) dup |= d.Q == c.Q && d.T == c.T && d.m == c.m && d.cta == c.cta && d.nb == c.nb;
       if (!dup) cand.push_back(c);
       if (cand.size() >= candidates) break;
     }
@@ -1656,7 +1699,7 @@ extern "C" int rs_plan_abcd(const char *text, size_t len, const rs_options *optp
   info->x_range = pl.X;
   info->baby_steps = pl.m;
   info->giant_steps = pl.T;
-  info->table_slots = (uint32_t)kBucket << pl.bucket_log2;
+  info->table_slots = (uint32_t)kBucket * pl.nbuckets;
   info->work_per_prime = pl.work_per_prime;
   info->warps_per_prime = pl.cta ? kCtaWarps : 1;
   info->row_form = plan_row_form(pl, s, nullptr);
@@ -1827,6 +1870,7 @@ void rs::job_release_buffers(rs_job *j) {
   j->d_chunk = nullptr;
   j->chunk_cap = 0;
   j->chunk_rec_elems = 0;
+  j->chunk_exact_bytes = 0;
   for (auto &pt : j->parts) {
     if (pt->d_hits) cudaFreeAsync(pt->d_hits, j->st);
     pt->d_hits = nullptr;

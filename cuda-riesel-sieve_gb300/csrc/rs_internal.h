@@ -97,7 +97,8 @@ struct JobDev {
   uint32_t tlanes;       // min(T, 32): lanes sharing one row
   uint32_t rows_per_it;  // 32 / tlanes
   uint32_t steps_per_lane;  // max(1, T / 32)
-  uint32_t table_log2;   // fast-path buckets per prime = 1 << table_log2
+  uint32_t table_log2;   // warp kernel: fast-path buckets per prime = 1 << table_log2
+  uint32_t nbuckets;     // fast-path buckets per prime (the CTA kernel: any multiple of 64)
   uint32_t jbits;        // bits of j in an exact-path table entry
   uint32_t nrows, nk;
   int64_t e0;            // x = e0 + m*s - j for giant index s in [1, T]
@@ -113,6 +114,7 @@ struct JobDev {
   uint32_t stage_full;   // 1 if V and row ids are read from the staged copy
   uint32_t warp_smem;    // shared-memory bytes per warp (bsgs_kernel) or per CTA (bsgs_cta_kernel)
   uint32_t exact_log2;   // slots of the exact kernel's table = 1 << exact_log2
+  uint32_t exact_global; // that table exceeds shared memory: it lives in ChunkBufs::exact_tab
   // device arrays
   const uint32_t *row_r;     // [nrows] n mod Q of each row
   const uint32_t *row_kidx;  // [nrows] index of the row's k
@@ -144,6 +146,7 @@ struct ChunkBufs {
   uint64_t *recs;       // [cap * rec_elems] records
   uint32_t *redo;       // [cap] primes handed to the exact BSGS kernel
   uint32_t *redo_count; // [1]
+  uint32_t *exact_tab;  // exact-kernel tables of jobs whose table exceeds shared memory (else null)
   uint32_t cap;
   // The baby step of the chunk: kStepSmall if every prime p of the chunk has
   // p > 2^33 and b^Q * p < 2^63 (the short product by the integer b^Q,
@@ -180,6 +183,7 @@ cudaError_t launch_bsgs_exact(const JobDev &job, const ChunkBufs &cb, const HitB
 cudaError_t launch_verify(const JobDev &job, const HitBufs &hb, cudaStream_t st);
 int bsgs_smem_bytes(const JobDev &job);
 int bsgs_exact_smem_bytes(const JobDev &job);
+uint64_t bsgs_exact_scratch_bytes(const JobDev &job, int exact_grid);
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out);
 
 cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,

@@ -599,18 +599,31 @@ __device__ __forceinline__ bool bucket_has(const uint4 &q, uint32_t T) {
 
 constexpr uint32_t kSlots = 8;  // tag slots per bucket
 
-// Hash-table view of one warp's shared memory: NB buckets of tags and NB 32-bit
+// Hash-table view of a prime's shared memory: NB buckets of tags and NB 32-bit
 // insert counts, kept apart from the buckets so that the counts of a warp's 32
 // random buckets spread over all 32 banks.  An insert takes slot c of its
 // bucket from an atomic add on the bucket's count and writes its tag there with
 // a plain 16-bit store.  Slots fill in order, so a bucket is full iff its slot 7
-// holds a tag, and an entry overflows into bucket b+1 only when bucket b is
-// full: a probe scans from the home bucket to the first bucket that is not full.
-struct WarpTable {
+// holds a tag, and an entry overflows into the next bucket only when its bucket
+// is full: a probe scans from the home bucket to the first bucket that is not
+// full.  The home bucket comes from the low 16 bits of a residue's low word and
+// the tag from the high 16 bits: the low bits masked when NB is a power of two
+// (MUL false), else scaled, (lo16 * NB) >> 16 (MUL true; any NB <= 65536), which
+// lets a CTA size its table to its shared memory instead of to a power of two.
+template <bool MUL>
+struct TableT {
   uint4 *tab4;
   uint16_t *tab16;
   uint32_t *cnt32;
-  uint32_t bmask;
+  uint32_t nb;     // buckets
+  uint32_t bmask;  // nb - 1 (MUL false)
+
+  __device__ __forceinline__ uint32_t home(uint32_t lo) const {
+    return MUL ? (uint32_t)(((lo & 0xffffu) * nb) >> 16) : (lo & bmask);
+  }
+  __device__ __forceinline__ uint32_t next(uint32_t b) const {
+    return MUL ? (b + 1 == nb ? 0u : b + 1) : ((b + 1) & bmask);
+  }
 
   __device__ __forceinline__ uint32_t take(uint32_t b) const {
     return atomicAdd(&cnt32[b], 1u);
@@ -620,8 +633,8 @@ struct WarpTable {
   __device__ __forceinline__ void insert_after(uint32_t lo, uint32_t b) const {
     uint32_t c = kSlots;
 #pragma unroll 1
-    for (uint32_t g = 0; c >= kSlots && g < bmask; g++) {
-      b = (b + 1) & bmask;
+    for (uint32_t g = 0; c >= kSlots && g + 1 < nb; g++) {
+      b = next(b);
       c = take(b);
     }
     if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
@@ -631,7 +644,7 @@ struct WarpTable {
   // insert later with insert_after, keeping the rare overflow off the hot loop).
   __device__ __forceinline__ bool insert_home(uint64_t v) const {
     const uint32_t lo = (uint32_t)v;
-    const uint32_t b = lo & bmask;
+    const uint32_t b = home(lo);
     const uint32_t c = take(b);
     if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
     return c < kSlots;
@@ -641,7 +654,7 @@ struct WarpTable {
   // is full (then only probe() can tell).
   __device__ __forceinline__ bool probe_home(uint64_t y) const {
     const uint32_t lo = (uint32_t)y;
-    const uint4 q = tab4[lo & bmask];
+    const uint4 q = tab4[home(lo)];
     const uint32_t T = tag_pair(lo);
     const uint32_t m = __vminu2(__vminu2(q.x ^ T, q.y ^ T), __vminu2(q.z ^ T, q.w ^ T));
     return (zero_half(m) | (q.w & 0xffff0000u)) != 0;  // a tag match, or slot 7 taken
@@ -650,14 +663,14 @@ struct WarpTable {
   // True iff some entry with the tag of y lies in y's probe sequence.
   __device__ __forceinline__ bool probe(uint64_t y) const {
     const uint32_t lo = (uint32_t)y;
-    uint32_t b = lo & bmask;
+    uint32_t b = home(lo);
     const uint32_t T = tag_pair(lo);
     uint4 q = tab4[b];
     bool hit = bucket_has(q, T);
     if (q.w >= 0x10000u) {  // the home bucket is full, continue scanning
 #pragma unroll 1
-      for (uint32_t g = 0; g < bmask; g++) {
-        b = (b + 1) & bmask;
+      for (uint32_t g = 0; g + 1 < nb; g++) {
+        b = next(b);
         q = tab4[b];
         hit |= bucket_has(q, T);
         if (q.w < 0x10000u) break;
@@ -666,6 +679,7 @@ struct WarpTable {
     return hit;
   }
 };
+using WarpTable = TableT<false>;
 
 struct MatchList {
   Match *list;
@@ -709,8 +723,8 @@ struct StepHigh {
 // Baby steps of one lane: two chains of `len` steps from va and vb, of which
 // the first na (nb) are inserted (all of them when FULL).  A value whose home bucket is full is
 // appended to ovf and inserted after the loop.
-template <bool FULL, class Step>
-__device__ __forceinline__ void baby_chains(const WarpTable &W, const MatchList &ML, uint64_t *ovf, uint64_t va,
+template <bool FULL, class Step, class Table>
+__device__ __forceinline__ void baby_chains(const Table &W, const MatchList &ML, uint64_t *ovf, uint64_t va,
                                             uint64_t vb, uint32_t na, uint32_t nb, uint32_t len, const Step &step) {
 #pragma unroll 4
   for (uint32_t t = 0; t < len; t++) {
@@ -815,6 +829,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   W.tab4 = reinterpret_cast<uint4 *>(base);
   W.tab16 = reinterpret_cast<uint16_t *>(base);
   W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
+  W.nb = NB;
   W.bmask = NB - 1;
   uint64_t *stage0 = reinterpret_cast<uint64_t *>(base + NB * 20);
   uint64_t *vbuf = stage0 + 2 * J.stage_elems;  // row_mask: V of the current prime
@@ -920,7 +935,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
         const uint64_t v = lane < novf ? ovf[lane] : 0;
         __syncwarp();
         if (lane == 0) *ML.count = 0;
-        if (lane < novf) W.insert_after((uint32_t)v, (uint32_t)v & W.bmask);
+        if (lane < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
         __syncwarp();
       }
 
@@ -1085,8 +1100,8 @@ int bsgs_smem_bytes(const JobDev &job) {
 // k*b^r come from the job's table ctab (kRowsIntId).  TWO (integer rows, spl == 2): the
 // second value of a slot is also c times a lane multiplier, Z advanced by G^32
 // (Glw2, Glq2), so both products are independent short ones.
-template <int RM, bool TWO>
-__device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &ML, const uint64_t *vst, uint32_t nact,
+template <int RM, bool TWO, class Table>
+__device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, const uint64_t *vst, uint32_t nact,
                                            uint32_t warp, uint32_t lane, uint32_t spl, uint64_t Glw, uint64_t Glq,
                                            uint64_t Gw, uint64_t Gq, uint64_t p, const uint32_t *__restrict__ ctab,
                                            uint64_t Glw2 = 0, uint64_t Glq2 = 0) {
@@ -1156,20 +1171,21 @@ __device__ __forceinline__ void cta_giants(const WarpTable &W, const MatchList &
 // V is staged with cp.async during the baby steps.  Table operations, the
 // deferred overflow inserts and the exact tag-match resolution are those of
 // bsgs_kernel; hits are pushed where they are found (tag matches are rare).
-template <int RM>
+template <int RM, bool MUL>
 __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
   constexpr uint32_t G = 32 * kCtaWarps;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t NB = 1u << J.table_log2;
+  const uint32_t NB = J.nbuckets;
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4);
-  WarpTable W;
+  TableT<MUL> W;
   W.tab4 = reinterpret_cast<uint4 *>(base);
   W.tab16 = reinterpret_cast<uint16_t *>(base);
   W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
+  W.nb = NB;
   W.bmask = NB - 1;
   uint64_t *vst = reinterpret_cast<uint64_t *>(base + NB * 20);
-  const uint32_t vst_elems = (J.max_act + 1) & ~1u;
+  const uint32_t vst_elems = RM == kRowsIntId ? 2 * ((J.max_act + 7) / 8) : (J.max_act + 1) & ~1u;
   MatchList ML;
   ML.list = reinterpret_cast<Match *>(vst + vst_elems);
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kCtaMatchCap);
@@ -1228,7 +1244,7 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
       const uint64_t v = tid < novf ? ovf[tid] : 0;
       __syncthreads();
       if (tid == 0) *ML.count = 0;
-      if (tid < novf) W.insert_after((uint32_t)v, (uint32_t)v & W.bmask);
+      if (tid < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
       __syncthreads();
     }
 
@@ -1294,7 +1310,10 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   const uint32_t grp = threadIdx.x / G, gt = threadIdx.x % G, wig = gt >> 5, lane = threadIdx.x & 31;
   const uint32_t S = 1u << J.exact_log2;
   const uint32_t tmask = S - 1;
-  uint32_t *tab = reinterpret_cast<uint32_t *>(smem4) + (size_t)grp * S;
+  // the table in shared memory, or (tables larger than shared memory) in this
+  // CTA's slice of the chunk's global scratch
+  uint32_t *tab = (J.exact_global ? cb.exact_tab + (size_t)blockIdx.x * NG * S : reinterpret_cast<uint32_t *>(smem4)) +
+                  (size_t)grp * S;
   const uint32_t jbits = J.jbits;
   const uint32_t jmask = (1u << jbits) - 1u;
   const uint32_t tagmask = (1u << (32 - jbits)) - 1u;
@@ -1375,7 +1394,12 @@ bsgs_exact_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 }
 
 int bsgs_exact_smem_bytes(const JobDev &job) {
-  return (job.cta_warps > 1 ? 1 : kWarpsPerBlock) * (4 << job.exact_log2);
+  return job.exact_global ? 0 : (job.cta_warps > 1 ? 1 : kWarpsPerBlock) * (4 << job.exact_log2);
+}
+
+uint64_t bsgs_exact_scratch_bytes(const JobDev &job, int exact_grid) {
+  if (!job.exact_global) return 0;
+  return (uint64_t)exact_grid * (job.cta_warps > 1 ? 1 : kWarpsPerBlock) * (4ull << job.exact_log2);
 }
 
 static cudaError_t configure_one(const void *fn, int smem, int threads, int device, int *grid_out) {
@@ -1403,12 +1427,18 @@ static cudaError_t configure_one(const void *fn, int smem, int threads, int devi
 
 static int bsgs_threads(const JobDev &job) { return job.cta_warps > 1 ? 32 * kCtaWarps : 32 * kWarpsPerBlock; }
 
-static BsgsFn bsgs_cta_fn(const JobDev &job) {
+template <bool MUL>
+static BsgsFn bsgs_cta_fn_t(const JobDev &job) {
   switch (row_mode(job)) {
-    case kRowsIntId: return bsgs_cta_kernel<kRowsIntId>;
-    case kRowsIntV: return bsgs_cta_kernel<kRowsIntV>;
-    default: return bsgs_cta_kernel<kRowsV>;
+    case kRowsIntId: return bsgs_cta_kernel<kRowsIntId, MUL>;
+    case kRowsIntV: return bsgs_cta_kernel<kRowsIntV, MUL>;
+    default: return bsgs_cta_kernel<kRowsV, MUL>;
   }
+}
+
+static BsgsFn bsgs_cta_fn(const JobDev &job) {
+  const bool pow2 = (job.nbuckets & (job.nbuckets - 1)) == 0;
+  return pow2 ? bsgs_cta_fn_t<false>(job) : bsgs_cta_fn_t<true>(job);
 }
 
 static const void *bsgs_fast_fn(const JobDev &job) {
@@ -1423,7 +1453,14 @@ static const void *bsgs_exact_fn(const JobDev &job) {
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out) {
   cudaError_t e = configure_one(bsgs_fast_fn(job), bsgs_smem_bytes(job), bsgs_threads(job), device, grid_out);
   if (e != cudaSuccess) return e;
-  return configure_one(bsgs_exact_fn(job), bsgs_exact_smem_bytes(job), bsgs_threads(job), device, exact_grid_out);
+  e = configure_one(bsgs_exact_fn(job), bsgs_exact_smem_bytes(job), bsgs_threads(job), device, exact_grid_out);
+  if (e != cudaSuccess) return e;
+  if (job.exact_global) {  // one CTA per SM keeps the global scratch small (the exact path is rare)
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess && sms > 0 && *exact_grid_out > sms) *exact_grid_out = sms;
+  }
+  return e;
 }
 
 cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &hb, int grid,
