@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference checkout.
 
-Run in a container where the reference is mounted at /root/reference:
-    python tests/golden/make_golden.py
+Run with the path of the reference's "CUDA Riesel Sieve" directory, as an
+argument or in the environment variable RSIEVE_REFERENCE_DIR:
+    python tests/golden/make_golden.py "<checkout>/CUDA Riesel Sieve"
 
 Writes
   sr_745.abcd  the reference's own test input ("CUDA Riesel Sieve/sr_745.abcd"),
@@ -26,7 +27,7 @@ import shutil
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/CUDA Riesel Sieve"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RSIEVE_REFERENCE_DIR", "")
 sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
 
 
@@ -113,4 +114,6 @@ def main() -> None:
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isfile(os.path.join(REF, "kernel_v0.24.6.cu")):
+        sys.exit("usage: make_golden.py <reference 'CUDA Riesel Sieve' directory> (or RSIEVE_REFERENCE_DIR)")
     main()
