@@ -505,15 +505,18 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
         // V staging: the integers k*b^r read by row id (two bytes a row) when a lane takes
         // two or more giant steps, else eight bytes a row (the row form of plan_row_form)
         const double vbytes = (ints_q && T >= 64 ? 2.0 : 8.0) * (rows + 2) + 16.0;
-        // buckets: a power of two with at most ~2 entries each, or any multiple of 64 with
-        // at most ~3 each (the table then fills the shared memory; overflow stays rare)
+        // buckets: a power of two with at most ~2 entries each, or, when that table does
+        // not fit the shared memory, the smallest multiple of 64 with at most ~2 each.
+        // (Tables at ~3 entries a bucket measured slower on the wide job, 183-216 against
+        // 174 ns per prime: more full buckets and more false tag matches.)
         const uint32_t blog = std::max<uint32_t>(4, ilog2_ceil((m + 1) / 2));
-        const uint32_t nb_opts[2] = {1u << blog, (uint32_t)std::max<uint64_t>(64, ((m + 2) / 3 + 63) / 64 * 64)};
+        const uint32_t nb_opts[2] = {1u << blog, (uint32_t)std::max<uint64_t>(64, ((m + 1) / 2 + 63) / 64 * 64)};
         for (int o = 0; o < 2; o++) {
           const uint32_t nbk = nb_opts[o];
-          if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536)) continue;
           const double nb = (double)nbk;
           const double smem = 20.0 * nb + vbytes + 16.0 * (kCtaMatchCap + 1);
+          if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536 || 20.0 * nb_opts[0] + vbytes + 16.0 * (kCtaMatchCap + 1) <= 232448.0))
+            continue;
           const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
           if (m <= mcap && m * T >= X && slog <= 17 && smem <= 232448.0 && fp <= 16.0) {
             const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +

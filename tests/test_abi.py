@@ -236,9 +236,8 @@ def test_plan_layouts(rs):
 def test_plan_row_forms(rs, sr745_text):
     """Giant-step start values: an active-row mask for the plain job (44 rows,
     every k*745 < 2^32, a warp per prime), the integers k*b^r in the records
-    for a warp-per-prime job with more than 64 rows and for the wide job (one
-    giant step per lane on the CTA kernel), read by row id for a CTA job with two
-    giant steps per lane, per-prime residues for
+    for a warp-per-prime job with more than 64 rows, read by row id for the wide
+    job and another CTA job with two giant steps per lane, per-prime residues for
     sr_745.abcd (Q = 18, so b^r is far above 2^32)."""
     import rsieve.synth as S
 
@@ -249,10 +248,7 @@ def test_plan_row_forms(rs, sr745_text):
     body = "\n".join(["1"] * 47 + [str(3 * 10**6 - 10**6 - 47)])
     wide = "".join(f"ABCD {k}*2^$a-1 [1000000]\n{body}\n" for k in range(3, 2003, 2))
     d = rs.plan_abcd(wide)
-    # the CTA table fills shared memory with a non-power-of-two bucket count, so the
-    # wide job balances at T = 32: one giant step per lane, k*b^r kept in V
-    assert (d["row_form"], d["warps_per_prime"], d["giant_steps"]) == (1, 16, 32)
-    assert d["table_slots"] % (8 * 64) == 0 and d["table_slots"] & (d["table_slots"] - 1) != 0
+    assert (d["row_form"], d["warps_per_prime"]) == (2, 16) and d["giant_steps"] >= 64
     (b, s, ks, nl), _ = S.batch_job(7, 8)
     d = rs.plan_abcd(S.to_abcd(b, s, ks, nl), datless=1)
     assert d["row_form"] == 2 and d["giant_steps"] >= 64
