@@ -1308,6 +1308,28 @@ static uint32_t chunk_step_form(const rs_job *j, const Part &pt, uint64_t a, uin
   return small_ok ? kStepSmall : high_ok ? kStepHigh : kStepShoup;
 }
 
+// Chunks [a, b] of [lo, hi] (lo odd) with an expected prime count of ~0.8*C each.
+struct Chunk {
+  uint64_t a, b;
+};
+static std::vector<Chunk> plan_chunks(uint64_t lo, uint64_t hi, uint32_t C) {
+  std::vector<Chunk> todo;
+  uint64_t a = lo;
+  while (a <= hi) {
+    const double la = std::log((double)a);
+    double w = la > 3.0 ? 0.8 * (double)C * (la - 1.2) : 1.6 * (double)C;
+    if (w < 64) w = 64;
+    if (w > 64.0 * (double)C) w = 64.0 * (double)C;
+    uint64_t width = (uint64_t)w & ~1ull;
+    uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
+    todo.push_back({a, b});
+    if (b >= hi) break;
+    a = b + 1;
+    if (!(a & 1)) a++;
+  }
+  return todo;
+}
+
 // One pass over [p0, p1]; returns kRetryHits after growing a part's hit
 // buffers when more candidate hits arrived than they could hold.
 //
@@ -1342,26 +1364,7 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
   }
   const uint32_t C = j->cb.cap;
 
-  // chunk list [a, b] with expected prime count ~0.8*C
-  struct Chunk {
-    uint64_t a, b;
-  };
-  std::vector<Chunk> todo;
-  {
-    uint64_t a = lo;
-    while (a <= hi) {
-      const double la = std::log((double)a);
-      double w = la > 3.0 ? 0.8 * (double)C * (la - 1.2) : 1.6 * (double)C;
-      if (w < 64) w = 64;
-      if (w > 64.0 * (double)C) w = 64.0 * (double)C;
-      uint64_t width = (uint64_t)w & ~1ull;
-      uint64_t b = (hi - a < width) ? hi : a + width - 1;  // a odd, width even -> b even or hi
-      todo.push_back({a, b});
-      if (b >= hi) break;
-      a = b + 1;
-      if (!(a & 1)) a++;
-    }
-  }
+  std::vector<Chunk> todo = plan_chunks(lo, hi, C);
 
   // timing events per chunk: before and after the sieve, then before setup,
   // before BSGS, before the exact kernel and after it, for every part
@@ -1655,6 +1658,431 @@ extern "C" int rs_job_autotune(rs_job *j, uint64_t p0, uint64_t p1, uint32_t can
   }
   set_chunk_cap(j);
   if (chosen) return rs_job_info_get(j, chosen);
+  return RS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: many jobs' ranges in rounds, one persistent BSGS launch per
+// kernel variant per round, each round recorded as a CUDA graph.
+
+struct rs_batch {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  struct Item {
+    rs_job *job = nullptr;
+    uint64_t p0 = 0, p1 = 0;
+    std::vector<rs_factor> out;
+    rs_stats st{};
+    int status = RS_OK;
+    std::string err;
+  };
+  std::vector<Item> items;
+  bool ran = false;
+};
+
+extern "C" int rs_batch_create(int device, rs_batch **out) {
+  if (!out) return fail(RS_ERR_INVALID, "rs_batch_create: NULL argument");
+  *out = nullptr;
+  int rc = check_device(device);
+  if (rc) return rc;
+  rs_batch *b = new rs_batch();
+  b->device = device;
+  const cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(RS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return RS_OK;
+}
+
+extern "C" int rs_batch_add(rs_batch *b, rs_job *job, uint64_t p0, uint64_t p1, uint32_t *item) {
+  if (!b || !job) return fail(RS_ERR_INVALID, "rs_batch_add: NULL argument");
+  if (job->device != b->device) return fail(RS_ERR_INVALID, "rs_batch_add: job on device %d, batch on %d", job->device,
+                                            b->device);
+  for (auto &it : b->items)
+    if (it.job == job) return fail(RS_ERR_INVALID, "rs_batch_add: the job is already in this batch");
+  if (b->items.size() >= 4096) return fail(RS_ERR_INVALID, "rs_batch_add: at most 4096 items");
+  if (p1 >= (1ull << 63)) return fail(RS_ERR_RANGE, "p1 must be < 2^63");
+  rs_batch::Item it;
+  it.job = job;
+  it.p0 = p0;
+  it.p1 = p1;
+  b->items.push_back(std::move(it));
+  b->ran = false;
+  if (item) *item = (uint32_t)(b->items.size() - 1);
+  return RS_OK;
+}
+
+// Kernel variant of a warp-per-prime part: items of one multi-job launch share it.
+static uint32_t batch_variant(const JobDev &d) {
+  const uint32_t rm = d.row_mask ? kRowsMask : d.row_ids_only ? kRowsIntId : d.int_rows ? kRowsIntV : kRowsV;
+  return d.tlanes * 8 + rm;
+}
+
+extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
+  if (!B) return fail(RS_ERR_INVALID, "rs_batch_run: NULL batch");
+  CUDA_TRY(cudaSetDevice(B->device));
+  rs_stats tot{};
+  // jobs locked for the whole run, in address order (a job is in one item only)
+  std::vector<rs_job *> order;
+  for (auto &it : B->items) order.push_back(it.job);
+  std::sort(order.begin(), order.end());
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (rs_job *j : order) locks.emplace_back(j->mu);
+
+  struct Run {  // a batched item: its chunks and their outcome
+    size_t item;
+    rs_job *j;
+    Part *pt;
+    uint64_t lo, hi;
+    std::vector<Chunk> chunks;
+    std::vector<uint32_t> forms;
+    size_t count0 = 0;  // first slot of its chunks in the pinned count array
+  };
+  std::vector<Run> runs;
+  std::vector<size_t> alone;  // items sieved through their own path (several parts)
+  for (size_t q = 0; q < B->items.size(); q++) {
+    auto &it = B->items[q];
+    it.out.clear();
+    it.st = rs_stats{};
+    it.status = RS_OK;
+    it.err.clear();
+    if (it.job->parts.size() != 1) {
+      alone.push_back(q);
+      continue;
+    }
+    uint64_t lo = it.p0 < 3 ? 3 : it.p0;
+    if (!(lo & 1)) lo++;
+    if (lo > it.p1) continue;
+    Run r;
+    r.item = q;
+    r.j = it.job;
+    r.pt = it.job->parts[0].get();
+    r.lo = lo;
+    r.hi = it.p1;
+    runs.push_back(std::move(r));
+  }
+  // device resources of every batched job, allocated before any recording
+  size_t nslots = 0;
+  for (Run &r : runs) {
+    rs_job *j = r.j;
+    int rc = ensure_sieving_primes(j, r.hi, &tot.h2d_bytes);
+    if (!rc) rc = ensure_chunk_buffers(j, j->cb.cap);
+    if (!rc && !r.pt->d_hits) rc = ensure_hit_buffers(j, *r.pt, 1u << 20);
+    if (rc) return rc;
+    r.chunks = plan_chunks(r.lo, r.hi, j->cb.cap);
+    uint64_t words = 0;
+    r.forms.resize(r.chunks.size());
+    for (size_t c = 0; c < r.chunks.size(); c++) {
+      words = std::max(words, sieve_bitmap_words(r.chunks[c].a, r.chunks[c].b));
+      r.forms[c] = chunk_step_form(j, *r.pt, r.chunks[c].a, r.chunks[c].b);
+    }
+    rc = ensure_gbits(j, words);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(j->st));
+    r.count0 = nslots;
+    nslots += r.chunks.size();
+  }
+  size_t rounds = 0;
+  for (Run &r : runs) rounds = std::max(rounds, r.chunks.size());
+  // groups of warp-per-prime runs sharing a kernel variant, and their launch shape
+  struct Group {
+    uint32_t variant;
+    std::vector<size_t> runs;
+    uint32_t stage_max = 0, tl_max = 0, warp_bytes = 0;
+    int grid = 0;
+  };
+  std::vector<Group> groups;
+  for (size_t r = 0; r < runs.size(); r++) {
+    const JobDev &d = runs[r].pt->dev;
+    if (d.cta_warps > 1) continue;
+    const uint32_t v = batch_variant(d);
+    size_t g = 0;
+    for (; g < groups.size() && groups[g].variant != v; g++) {
+    }
+    if (g == groups.size()) groups.push_back(Group{v, {}});
+    groups[g].runs.push_back(r);
+    groups[g].stage_max = std::max(groups[g].stage_max, d.stage_elems);
+    groups[g].tl_max = std::max(groups[g].tl_max, d.table_log2);
+  }
+  // the launch items of every (round, group), written once and copied to the device once
+  std::vector<std::vector<size_t>> goff(rounds, std::vector<size_t>(groups.size(), 0));
+  std::vector<std::vector<uint32_t>> gn(rounds, std::vector<uint32_t>(groups.size(), 0));
+  std::vector<BatchItem> hitems;
+  for (size_t rd = 0; rd < rounds; rd++)
+    for (size_t g = 0; g < groups.size(); g++) {
+      goff[rd][g] = hitems.size();
+      for (size_t r : groups[g].runs) {
+        Run &R = runs[r];
+        if (rd >= R.chunks.size()) continue;
+        BatchItem x;
+        x.J = R.pt->dev;
+        x.cb = R.j->cb;
+        x.cb.small_step = R.forms[rd];
+        x.hb = R.pt->hb;
+        hitems.push_back(x);
+        gn[rd][g]++;
+      }
+      if (gn[rd][g] > kBatchMaxItems) return fail(RS_ERR_INVALID, "rs_batch_run: more than %u jobs of one kernel variant",
+                                                  kBatchMaxItems);
+    }
+  for (Group &g : groups) {
+    g.warp_bytes = batch_warp_bytes(g.stage_max, g.tl_max);
+    CUDA_TRY(batch_configure(runs[g.runs[0]].pt->dev, g.warp_bytes, B->device, &g.grid));
+  }
+  BatchItem *d_items = nullptr;
+  uint32_t *h_counts = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto cleanup = [&]() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (d_items) cudaFreeAsync(d_items, B->st);
+    if (h_counts) pinned_put(h_counts, (nslots + 1) * 4);
+    cudaStreamSynchronize(B->st);
+  };
+  h_counts = (uint32_t *)pinned_get((nslots + 1) * 4);
+  if (!h_counts) return fail(RS_ERR_NOMEM, "cudaMallocHost failed");
+  if (!hitems.empty()) {
+    if (cudaMallocAsync(&d_items, hitems.size() * sizeof(BatchItem), B->st) != cudaSuccess ||
+        cudaMemcpyAsync(d_items, hitems.data(), hitems.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, B->st) !=
+            cudaSuccess) {
+      cleanup();
+      return fail(RS_ERR_CUDA, "rs_batch_run: batch item upload failed");
+    }
+    tot.h2d_bytes += hitems.size() * sizeof(BatchItem);
+  }
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  for (Run &R : runs) {
+    cudaMemsetAsync(R.pt->hb.raw_count, 0, 4, B->st);
+    cudaMemsetAsync(R.pt->hb.fac_count, 0, 4, B->st);
+    cudaMemsetAsync(R.pt->hb.stat, 0, kStatCount * sizeof(unsigned long long), B->st);
+  }
+  cudaEventRecord(ev0, B->st);
+  // the rounds, each recorded on the batch stream and launched as one graph
+  cudaError_t e = cudaSuccess;
+  for (size_t rd = 0; rd < rounds && e == cudaSuccess; rd++) {
+    e = cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) break;
+    for (Run &R : runs) {
+      if (rd >= R.chunks.size()) continue;
+      rs_job *j = R.j;
+      const Chunk &c = R.chunks[rd];
+      cudaMemsetAsync(j->cb.count, 0, 4, B->st);
+      launch_sieve(c.a, c.b, j->d_sp, j->d_sp_rcp, j->nsp, j->nsp_small, j->d_gbits, j->cb.primes, j->cb.count,
+                   j->cb.cap, B->st);
+      cudaMemcpyAsync(&h_counts[R.count0 + rd], j->cb.count, 4, cudaMemcpyDeviceToHost, B->st);
+      ChunkBufs cb = j->cb;
+      cb.small_step = R.forms[rd];
+      launch_setup(R.pt->dev, cb, B->st);
+      cudaMemsetAsync(j->cb.redo_count, 0, 4, B->st);
+      tot.launches += (j->nsp > j->nsp_small ? 2 : 1) + 1;
+    }
+    for (size_t g = 0; g < groups.size(); g++) {
+      if (!gn[rd][g]) continue;
+      launch_bsgs_batch(runs[groups[g].runs[0]].pt->dev, d_items + goff[rd][g], gn[rd][g], groups[g].stage_max,
+                        groups[g].warp_bytes, groups[g].grid, B->st);
+      tot.launches++;
+      tot.bsgs_launches++;
+    }
+    for (Run &R : runs) {
+      if (rd >= R.chunks.size()) continue;
+      ChunkBufs cb = R.j->cb;
+      cb.small_step = R.forms[rd];
+      if (R.pt->dev.cta_warps > 1) {
+        launch_bsgs(R.pt->dev, cb, R.pt->hb, R.pt->bsgs_grid, B->st);
+        tot.launches++;
+        tot.bsgs_launches++;
+      }
+      launch_bsgs_exact(R.pt->dev, cb, R.pt->hb, R.pt->exact_grid, B->st);
+      tot.launches++;
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(B->st, &graph);
+    if (e != cudaSuccess) break;
+    if (exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+      }
+    }
+    if (!exec) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, B->st);
+    cudaGraphDestroy(graph);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->st);
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(RS_ERR_CUDA, "rs_batch_run rounds: %s", cudaGetErrorString(e));
+  }
+  // verification, then every batched item's factors
+  for (Run &R : runs) {
+    e = launch_verify(R.pt->dev, R.pt->hb, B->st);
+    tot.launches++;
+    if (e != cudaSuccess) break;
+  }
+  cudaEventRecord(ev1, B->st);
+  std::vector<uint32_t> counts(2 * runs.size());
+  std::vector<unsigned long long> dstat(kStatCount * runs.size());
+  for (size_t r = 0; r < runs.size() && e == cudaSuccess; r++) {
+    const HitBufs &hb = runs[r].pt->hb;
+    e = cudaMemcpyAsync(&counts[2 * r], hb.raw_count, 4, cudaMemcpyDeviceToHost, B->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&counts[2 * r + 1], hb.fac_count, 4, cudaMemcpyDeviceToHost, B->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&dstat[kStatCount * r], hb.stat, kStatCount * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, B->st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->st);
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(RS_ERR_CUDA, "rs_batch_run verify: %s", cudaGetErrorString(e));
+  }
+  {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    tot.gpu_ms = ms;
+  }
+  for (size_t r = 0; r < runs.size(); r++) {
+    Run &R = runs[r];
+    auto &it = B->items[R.item];
+    rs_job *j = R.j;
+    rs_stats &st = it.st;
+    // chunks with more primes than the buffer held are sieved again through the
+    // job's own path; so is the whole item when its hit buffer overflowed
+    std::vector<Chunk> again;
+    for (size_t c = 0; c < R.chunks.size(); c++) {
+      const uint32_t n = h_counts[R.count0 + c];
+      if (n > j->cb.cap) {
+        again.push_back(R.chunks[c]);
+      } else {
+        st.primes += n;
+        const uint32_t f = R.forms[c];
+        st.primes_by_step[f == kStepShoup ? 0 : f == kStepSmall ? 1 : 2] += n;
+      }
+    }
+    if (counts[2 * r] > R.pt->hb.cap) {
+      again.assign(1, Chunk{R.lo, R.hi});
+      st = rs_stats{};
+    } else {
+      st.raw_hits = counts[2 * r];
+      st.paired_primes = dstat[kStatCount * r + kStatPaired];
+      st.exact_primes = dstat[kStatCount * r + kStatExact];
+      const uint32_t nf = counts[2 * r + 1];
+      std::vector<Hit> h(nf);
+      if (nf) {
+        e = cudaMemcpy(h.data(), R.pt->hb.fac, nf * sizeof(Hit), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+          cleanup();
+          return fail(RS_ERR_CUDA, "rs_batch_run factors: %s", cudaGetErrorString(e));
+        }
+        tot.d2h_bytes += nf * sizeof(Hit);
+      }
+      const uint32_t base = R.pt->seqs.base;
+      const int32_t sign = R.pt->seqs.sign;
+      for (const Hit &x : h) it.out.push_back(rs_factor{x.p, x.k, x.n, base, sign});
+    }
+    for (const Chunk &c : again) {  // rare: through the job's own path
+      std::vector<rs_factor> more(1 << 12);
+      size_t cnt = 0;
+      rs_stats s2{};
+      int rc = kRetryHits;
+      for (int attempt = 0; attempt < 4 && (rc == kRetryHits || rc == RS_ERR_CAPACITY); attempt++) {
+        rc = sieve_range_impl(j, c.a, c.b, more.data(), more.size(), &cnt, &s2);
+        if (rc == RS_ERR_CAPACITY) more.resize(cnt);
+      }
+      if (rc) {
+        it.status = rc;
+        it.err = rs_last_error();
+        break;
+      }
+      it.out.insert(it.out.end(), more.begin(), more.begin() + cnt);
+      st.primes += s2.primes;
+      st.raw_hits += s2.raw_hits;
+      for (int f = 0; f < 3; f++) st.primes_by_step[f] += s2.primes_by_step[f];
+      st.paired_primes += s2.paired_primes;
+      st.exact_primes += s2.exact_primes;
+      tot.launches += s2.launches;
+    }
+    std::sort(it.out.begin(), it.out.end(), [](const rs_factor &a, const rs_factor &b) {
+      return std::tie(a.p, a.k, a.n, a.b, a.c) < std::tie(b.p, b.k, b.n, b.b, b.c);
+    });
+    it.out.erase(std::unique(it.out.begin(), it.out.end(),
+                             [](const rs_factor &a, const rs_factor &b) {
+                               return a.p == b.p && a.k == b.k && a.n == b.n && a.b == b.b && a.c == b.c;
+                             }),
+                 it.out.end());
+    if (it.status == RS_OK && j->opt.host_verify)
+      for (const rs_factor &f : it.out)
+        if (!host_verify(f.p, f.k, f.b, f.n, f.c)) {
+          it.status = RS_ERR_INTERNAL;
+          it.err = "a factor failed host verification";
+          break;
+        }
+    st.factors = it.out.size();
+    st.p_covered = R.hi - R.lo + 1;
+  }
+  cleanup();
+  // jobs of several parts: their own path
+  for (size_t q : alone) {
+    auto &it = B->items[q];
+    std::vector<rs_factor> out(1 << 12);
+    size_t cnt = 0;
+    int rc = kRetryHits;
+    for (int attempt = 0; attempt < 4 && (rc == kRetryHits || rc == RS_ERR_CAPACITY); attempt++) {
+      rc = sieve_range_impl(it.job, it.p0, it.p1, out.data(), out.size(), &cnt, &it.st);
+      if (rc == RS_ERR_CAPACITY) out.resize(cnt);
+    }
+    if (rc) {
+      it.status = rc;
+      it.err = rs_last_error();
+    } else {
+      it.out.assign(out.begin(), out.begin() + cnt);
+      tot.gpu_ms += it.st.gpu_ms;
+      tot.launches += it.st.launches;
+    }
+  }
+  for (auto &it : B->items) {
+    tot.primes += it.st.primes;
+    tot.factors += it.out.size();
+    tot.raw_hits += it.st.raw_hits;
+    tot.p_covered += it.st.p_covered;
+    for (int f = 0; f < 3; f++) tot.primes_by_step[f] += it.st.primes_by_step[f];
+    tot.paired_primes += it.st.paired_primes;
+    tot.exact_primes += it.st.exact_primes;
+  }
+  if (stats) *stats = tot;
+  B->ran = true;
+  for (auto &it : B->items)
+    if (it.status != RS_OK) return fail(it.status, "rs_batch_run: an item failed: %s", it.err.c_str());
+  return RS_OK;
+}
+
+extern "C" int rs_batch_result(const rs_batch *B, uint32_t item, rs_factor *out, size_t cap, size_t *count,
+                               rs_stats *stats) {
+  if (!B || !count || (!out && cap)) return fail(RS_ERR_INVALID, "rs_batch_result: NULL argument");
+  if (item >= B->items.size()) return fail(RS_ERR_INVALID, "rs_batch_result: no item %u", item);
+  if (!B->ran) return fail(RS_ERR_INVALID, "rs_batch_result: the batch has not run");
+  const auto &it = B->items[item];
+  if (stats) *stats = it.st;
+  *count = it.out.size();
+  if (it.status != RS_OK) return fail(it.status, "%s", it.err.c_str());
+  if (it.out.size() > cap) return fail(RS_ERR_CAPACITY, "%zu factors, buffer holds %zu", it.out.size(), cap);
+  if (!it.out.empty()) memcpy(out, it.out.data(), it.out.size() * sizeof(rs_factor));
+  return RS_OK;
+}
+
+extern "C" int rs_batch_destroy(rs_batch *B) {
+  if (!B) return RS_OK;
+  if (B->st) {
+    cudaStreamSynchronize(B->st);
+    cudaStreamDestroy(B->st);
+  }
+  delete B;
   return RS_OK;
 }
 

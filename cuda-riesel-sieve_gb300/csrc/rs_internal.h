@@ -167,6 +167,16 @@ constexpr int kStatPaired = 0;  // primes whose giant loop took the (k, 0), (k, 
 constexpr int kStatExact = 1;   // primes finished by the exact kernel
 constexpr int kStatCount = 2;
 
+// One job's chunk in a multi-job BSGS launch (the batched form): its constants,
+// its chunk of primes and records, its hit buffers.  Items of one launch share
+// the warp-per-prime layout, the giant lanes (tlanes) and the start-value form.
+struct BatchItem {
+  JobDev J;
+  ChunkBufs cb;
+  HitBufs hb;
+};
+constexpr uint32_t kBatchMaxItems = 256;  // items of one multi-job launch
+
 // Launchers (rs_kernels.cu).  All enqueue on `st` and return the launch status.
 // Odd primes of [lo, hi] (lo odd) appended to out[] (count may exceed cap).
 // sp: odd primes up to sqrt(hi), ascending, with rcp = floor(2^64/q); the first
@@ -185,6 +195,13 @@ int bsgs_smem_bytes(const JobDev &job);
 int bsgs_exact_smem_bytes(const JobDev &job);
 uint64_t bsgs_exact_scratch_bytes(const JobDev &job, int exact_grid);
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out);
+// Multi-job launch over `nitems` items in device memory that share rep's kernel
+// variant (rep: any of them); stage_max and table_log2_max are the largest over
+// the items.  batch_configure gives its per-warp shared memory and grid.
+uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max);
+cudaError_t batch_configure(const JobDev &rep, uint32_t warp_bytes, int device, int *grid_out);
+cudaError_t launch_bsgs_batch(const JobDev &rep, const BatchItem *items, uint32_t nitems, uint32_t stage_max,
+                              uint32_t warp_bytes, int grid, cudaStream_t st);
 
 cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
                                  uint32_t total_words, uint32_t *bits, cudaStream_t st);

@@ -802,6 +802,199 @@ __device__ __forceinline__ void giant_home_int(const WarpTable &W, const uint16_
   }
 }
 
+// The work of one prime in the warp-per-prime layout, the whole warp together:
+// baby steps into the table, giant steps with home-bucket tests, deferred
+// probes, and the exact resolution of tag matches.  cur is the prime's staged
+// record (header, and V or the row mask; nact != 0), Bl and Glm the lane's two
+// table entries, c_lo / c_hi (row_mask) the lane's row constants; npaired
+// counts the primes that took the row-pair path.  Shared by the single-job
+// kernel and the multi-job kernel below.
+template <int TL, int RM>
+__device__ __forceinline__ void bsgs_prime(const JobDev &J, const ChunkBufs &cb, const HitBufs &hb,
+                                           const WarpTable &W, const MatchList &ML, uint64_t *vbuf,
+                                           const uint64_t *cur, uint32_t i, uint32_t nact, uint64_t Bl,
+                                           uint64_t Glm, uint32_t lane, uint32_t c_lo, uint32_t c_hi,
+                                           uint32_t &npaired) {
+  constexpr uint32_t RPI = 32 / TL;  // row slots per lane-group pass
+  const uint32_t lane_t = lane & (TL - 1);
+  const uint32_t lane_row = lane / TL;
+  const uint32_t spl = J.steps_per_lane;
+  if constexpr (RM == kRowsMask) {  // V from the active-row mask
+    const uint64_t am = cur[kElV];
+    const uint32_t lo = (uint32_t)am, hi = (uint32_t)(am >> 32), below = (1u << lane) - 1u;
+    if ((lo >> lane) & 1u) vbuf[__popc(lo & below)] = c_lo;
+    if ((hi >> lane) & 1u) vbuf[__popc(lo) + __popc(hi & below)] = c_hi;
+  }
+  const uint64_t p = cur[kElP], pinv = cur[kElPinv];
+  // Multipliers in normal form with their Shoup constants; the values
+  // they multiply stay in Montgomery form, so products stay comparable.
+  const uint64_t Stw = cur[kElStw], Stq = cur[kElStq];
+  const uint64_t Gw = cur[kElGw], Gq = cur[kElGq];
+  const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
+  // chain starts B^(lane*CL) and B^((lane+32)*CL); valid steps na, nb (j < m)
+  const uint32_t CL = J.chain_len;
+  const uint32_t ja0 = lane * CL, jb0 = ja0 + 32 * CL;
+  const uint32_t na = J.m > ja0 ? min(CL, J.m - ja0) : 0;
+  const uint32_t nb = J.m > jb0 ? min(CL, J.m - jb0) : 0;
+  const uint64_t Blb = shoup_mul(Bl, cur[kElOfw], cur[kElOfq], p);
+  // clear the table (tags and counts)
+  const uint4 z4 = make_uint4(0, 0, 0, 0);
+#pragma unroll 4
+  for (uint32_t q = lane; q < W.nb + W.nb / 4; q += 32) W.tab4[q] = z4;
+  if (lane == 0) *ML.count = 0;
+  __syncwarp();
+
+  // Baby steps: chain A owns j = ja0 + t, chain B j = jb0 + t.  Values whose
+  // home bucket is full go to a short list (the match list's space, unused
+  // until the giant steps) and are inserted after the loop.
+  uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
+  if (J.m == 64 * CL) {  // every chain full (the planner's usual choice of m)
+    // (kStepHigh chunks take Shoup's product here: a third baby loop in this
+    // kernel measured slower on the short-product path)
+    if (cb.small_step == kStepSmall)
+      baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
+    else
+      baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
+  } else {
+    if (cb.small_step == kStepSmall)
+      baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
+    else
+      baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
+  }
+  __syncwarp();
+  const uint32_t novf = *ML.count;
+  if (novf > 2 * ML.cap) {  // pathological table: leave the prime to the exact path
+    if (lane == 0) {
+      const uint32_t r = atomicAdd(cb.redo_count, 1u);
+      if (r < cb.cap) cb.redo[r] = i;
+    }
+    __syncwarp();
+    return;
+  }
+  if (novf) {
+    const uint64_t v = lane < novf ? ovf[lane] : 0;
+    __syncwarp();
+    if (lane == 0) *ML.count = 0;
+    if (lane < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
+    __syncwarp();
+  }
+
+  // Giant steps: lane (lane_row, lane_t) takes row slots g*RPI + lane_row for
+  // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
+  const uint32_t ngi = (nact + RPI - 1) / RPI;
+  const uint64_t *Vs = J.stage_full ? cur + kElV : cb.recs + (size_t)i * J.rec_elems + kElV;
+  // integer rows: the row ids (16 bits) of the staged or global record
+  const uint16_t *Rs = reinterpret_cast<const uint16_t *>(
+      J.stage_full ? cur + J.el_row : cb.recs + (size_t)i * J.rec_elems + J.el_row);
+  // the giant value of slot sl (the general and the integer-row form)
+  auto giant_val = [&](uint32_t sl) -> uint64_t {
+    if constexpr (RM == kRowsIntId) return shoup_mul32(__ldg(J.row_c + Rs[sl]), Glw, Glq, p);
+    else if constexpr (RM == kRowsIntV) return shoup_mul32((uint32_t)Vs[sl], Glw, Glq, p);
+    else if constexpr (RM == kRowsMask) return shoup_mul32((uint32_t)vbuf[sl], Glw, Glq, p);
+    else return shoup_mul(Vs[sl], Glw, Glq, p);
+  };
+  if (spl == 1 && ngi <= 64) {
+    // One giant step per slot.  The loop only tests each value's home
+    // bucket and collects the outcome as bits (pass gi of chain A or B ->
+    // bit gi/2); tag hits and full home buckets are finished after it.
+    // Separate calls for staged and global V keep each load's address
+    // space known to the compiler.
+    uint32_t hA = 0, hB = 0;
+    const bool paired = RPI == 1 && cb.small_step == kStepSmall && (cur[kElNact] >> 32);
+    npaired += paired && J.stage_full;
+    if constexpr (RM == kRowsIntId) {
+      const uint16_t *Rst = reinterpret_cast<const uint16_t *>(cur + J.el_row);
+      if (paired && J.stage_full)
+        giant_home_int<RPI, RPI == 1>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                      (uint32_t)cur[kElRcp]);
+      else if (J.stage_full)
+        giant_home_int<RPI>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+      else
+        giant_home_int<RPI>(W, Rs, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+    } else {
+      constexpr bool INT = RM == kRowsIntV || RM == kRowsMask;
+      const uint64_t *Vst = RM == kRowsMask ? vbuf : cur + kElV;  // V in shared memory
+      if (paired && J.stage_full)
+        giant_home<RPI, RPI == 1, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
+                                       (uint32_t)cur[kElRcp]);
+      else if (J.stage_full)
+        giant_home<RPI, false, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+      else
+        giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
+    }
+    if (hA | hB) {
+#pragma unroll 1
+      for (uint32_t h = 0; h < 2; h++) {
+        uint32_t bits = h ? hB : hA;
+        while (bits) {
+          const uint32_t g = 2 * (__ffs(bits) - 1) + h;
+          bits &= bits - 1;
+          const uint32_t sl = g * RPI + lane_row;
+          if (sl < nact) {
+            const uint64_t y = giant_val(sl);
+            if (W.probe(y)) ML.push(y, sl, lane_t + 1);
+          }
+        }
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (uint32_t gi = 0; gi < ngi; gi += 2) {
+      const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
+      const bool aa = sa < nact, ab = sb < nact;
+      uint64_t ya = giant_val(min(sa, nact - 1));
+      uint64_t yb = giant_val(min(sb, nact - 1));
+      uint32_t s = lane_t + 1;
+#pragma unroll 1
+      for (uint32_t u = 0;; u++) {
+        if (W.probe(ya) && aa) ML.push(ya, sa, s);
+        if (W.probe(yb) && ab) ML.push(yb, sb, s);
+        if (u + 1 >= spl) break;
+        ya = shoup_mul(ya, Gw, Gq, p);
+        yb = shoup_mul(yb, Gw, Gq, p);
+        s += 32;
+      }
+    }
+  }
+  __syncwarp();
+
+  // Tag matches: recompute the baby steps and compare full 64-bit values.
+  const uint32_t mc = *ML.count;
+  if (mc > (uint32_t)kMatchCap) {
+    if (lane == 0) {
+      const uint32_t r = atomicAdd(cb.redo_count, 1u);
+      if (r < cb.cap) cb.redo[r] = i;
+    }
+  } else if (mc > 0) {
+    uint64_t va = Bl, vb = Blb;
+#pragma unroll 1
+    for (uint32_t t = 0; t < CL; t++) {
+#pragma unroll 1
+      for (uint32_t h = 0; h < 2; h++) {
+        const uint64_t v = h ? vb : va;
+        if (t < (h ? nb : na)) {
+#pragma unroll 1
+          for (uint32_t q = 0; q < mc; q++) {
+            const Match mt = ML.list[q];
+            if (mt.y == v) {
+              uint32_t row;
+              if constexpr (RM == kRowsMask) {
+                row = nth_row(cur[kElV], mt.slot);
+              } else {
+                const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
+              }
+              record_hit(J, hb, p, row, mt.s, (h ? jb0 : ja0) + t);
+            }
+          }
+        }
+      }
+      va = shoup_mul(va, Stw, Stq, p);
+      vb = shoup_mul(vb, Stw, Stq, p);
+    }
+  }
+}
+
 // Per-warp shared memory of the fast kernel:
 //   [NB buckets x 16 B][NB counts x 4 B][2 stages x stage_elems x 8 B]
 //   ([kMaskRows V x 8 B], row_mask only)[kMatchCap matches][count, 16 B]
@@ -821,7 +1014,6 @@ template <int TL, int RM>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   extern __shared__ uint4 smem4[];
-  constexpr uint32_t RPI = 32 / TL;  // row slots per lane-group pass
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t NB = 1u << J.table_log2;
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * J.warp_smem;
@@ -837,13 +1029,10 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
   ML.list = reinterpret_cast<Match *>(vbuf + (RM == kRowsMask ? kMaskRows : 0));
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
   ML.cap = kMatchCap;
-  const uint32_t lane_t = lane & (TL - 1);
-  const uint32_t lane_row = lane / TL;
   const uint32_t total = *cb.count;
   const uint32_t n = total < cb.cap ? total : cb.cap;
   const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
   const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
-  const uint32_t spl = J.steps_per_lane;
   const uint64_t *ltab = cb.recs + J.el_tab + lane;  // this lane's B^lane; G^(lane+1) 32 further
 
   uint64_t nBl = 0, nGl = 0;
@@ -878,186 +1067,127 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
     stage_wait_prev();
     __syncwarp();
     const uint32_t nact = (uint32_t)cur[kElNact];
-    if (nact != 0) {
-      if constexpr (RM == kRowsMask) {  // V from the active-row mask
-        const uint64_t am = cur[kElV];
-        const uint32_t lo = (uint32_t)am, hi = (uint32_t)(am >> 32), below = (1u << lane) - 1u;
-        if ((lo >> lane) & 1u) vbuf[__popc(lo & below)] = c_lo;
-        if ((hi >> lane) & 1u) vbuf[__popc(lo) + __popc(hi & below)] = c_hi;
-      }
-      const uint64_t p = cur[kElP], pinv = cur[kElPinv];
-      // Multipliers in normal form with their Shoup constants; the values
-      // they multiply stay in Montgomery form, so products stay comparable.
-      const uint64_t Stw = cur[kElStw], Stq = cur[kElStq];
-      const uint64_t Gw = cur[kElGw], Gq = cur[kElGq];
-      const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
-      // chain starts B^(lane*CL) and B^((lane+32)*CL); valid steps na, nb (j < m)
-      const uint32_t CL = J.chain_len;
-      const uint32_t ja0 = lane * CL, jb0 = ja0 + 32 * CL;
-      const uint32_t na = J.m > ja0 ? min(CL, J.m - ja0) : 0;
-      const uint32_t nb = J.m > jb0 ? min(CL, J.m - jb0) : 0;
-      const uint64_t Blb = shoup_mul(Bl, cur[kElOfw], cur[kElOfq], p);
-      // clear the table (tags and counts)
-      const uint4 z4 = make_uint4(0, 0, 0, 0);
-#pragma unroll 4
-      for (uint32_t q = lane; q < NB + NB / 4; q += 32) W.tab4[q] = z4;
-      if (lane == 0) *ML.count = 0;
-      __syncwarp();
-
-      // Baby steps: chain A owns j = ja0 + t, chain B j = jb0 + t.  Values whose
-      // home bucket is full go to a short list (the match list's space, unused
-      // until the giant steps) and are inserted after the loop.
-      uint64_t *ovf = reinterpret_cast<uint64_t *>(ML.list);
-      if (J.m == 64 * CL) {  // every chain full (the planner's usual choice of m)
-        // (kStepHigh chunks take Shoup's product here: a third baby loop in this
-        // kernel measured slower on the short-product path)
-        if (cb.small_step == kStepSmall)
-          baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
-        else
-          baby_chains<true>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
-      } else {
-        if (cb.small_step == kStepSmall)
-          baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepSmall{J.bq_small, (uint32_t)cur[kElRcp], p});
-        else
-          baby_chains<false>(W, ML, ovf, Bl, Blb, na, nb, CL, StepShoup{Stw, Stq, p});
-      }
-      __syncwarp();
-      const uint32_t novf = *ML.count;
-      if (novf > 2 * ML.cap) {  // pathological table: leave the prime to the exact path
-        if (lane == 0) {
-          const uint32_t r = atomicAdd(cb.redo_count, 1u);
-          if (r < cb.cap) cb.redo[r] = i;
-        }
-        __syncwarp();
-        continue;
-      }
-      if (novf) {
-        const uint64_t v = lane < novf ? ovf[lane] : 0;
-        __syncwarp();
-        if (lane == 0) *ML.count = 0;
-        if (lane < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
-        __syncwarp();
-      }
-
-      // Giant steps: lane (lane_row, lane_t) takes row slots g*RPI + lane_row for
-      // two consecutive passes g at a time, giant indices s = lane_t + 1 (+32).
-      const uint32_t ngi = (nact + RPI - 1) / RPI;
-      const uint64_t *Vs = J.stage_full ? cur + kElV : cb.recs + (size_t)i * J.rec_elems + kElV;
-      // integer rows: the row ids (16 bits) of the staged or global record
-      const uint16_t *Rs = reinterpret_cast<const uint16_t *>(
-          J.stage_full ? cur + J.el_row : cb.recs + (size_t)i * J.rec_elems + J.el_row);
-      // the giant value of slot sl (the general and the integer-row form)
-      auto giant_val = [&](uint32_t sl) -> uint64_t {
-        if constexpr (RM == kRowsIntId) return shoup_mul32(__ldg(J.row_c + Rs[sl]), Glw, Glq, p);
-        else if constexpr (RM == kRowsIntV) return shoup_mul32((uint32_t)Vs[sl], Glw, Glq, p);
-        else if constexpr (RM == kRowsMask) return shoup_mul32((uint32_t)vbuf[sl], Glw, Glq, p);
-        else return shoup_mul(Vs[sl], Glw, Glq, p);
-      };
-      if (spl == 1 && ngi <= 64) {
-        // One giant step per slot.  The loop only tests each value's home
-        // bucket and collects the outcome as bits (pass gi of chain A or B ->
-        // bit gi/2); tag hits and full home buckets are finished after it.
-        // Separate calls for staged and global V keep each load's address
-        // space known to the compiler.
-        uint32_t hA = 0, hB = 0;
-        const bool paired = RPI == 1 && cb.small_step == kStepSmall && (cur[kElNact] >> 32);
-        npaired += paired && J.stage_full;
-        if constexpr (RM == kRowsIntId) {
-          const uint16_t *Rst = reinterpret_cast<const uint16_t *>(cur + J.el_row);
-          if (paired && J.stage_full)
-            giant_home_int<RPI, RPI == 1>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
-                                          (uint32_t)cur[kElRcp]);
-          else if (J.stage_full)
-            giant_home_int<RPI>(W, Rst, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
-          else
-            giant_home_int<RPI>(W, Rs, J.row_c, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
-        } else {
-          constexpr bool INT = RM == kRowsIntV || RM == kRowsMask;
-          const uint64_t *Vst = RM == kRowsMask ? vbuf : cur + kElV;  // V in shared memory
-          if (paired && J.stage_full)
-            giant_home<RPI, RPI == 1, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB, J.base,
-                                           (uint32_t)cur[kElRcp]);
-          else if (J.stage_full)
-            giant_home<RPI, false, INT>(W, Vst, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
-          else
-            giant_home<RPI, false, INT>(W, Vs, ngi, nact, lane_row, Glw, Glq, p, hA, hB);
-        }
-        if (hA | hB) {
-#pragma unroll 1
-          for (uint32_t h = 0; h < 2; h++) {
-            uint32_t bits = h ? hB : hA;
-            while (bits) {
-              const uint32_t g = 2 * (__ffs(bits) - 1) + h;
-              bits &= bits - 1;
-              const uint32_t sl = g * RPI + lane_row;
-              if (sl < nact) {
-                const uint64_t y = giant_val(sl);
-                if (W.probe(y)) ML.push(y, sl, lane_t + 1);
-              }
-            }
-          }
-        }
-      } else {
-#pragma unroll 1
-        for (uint32_t gi = 0; gi < ngi; gi += 2) {
-          const uint32_t sa = gi * RPI + lane_row, sb = sa + RPI;
-          const bool aa = sa < nact, ab = sb < nact;
-          uint64_t ya = giant_val(min(sa, nact - 1));
-          uint64_t yb = giant_val(min(sb, nact - 1));
-          uint32_t s = lane_t + 1;
-#pragma unroll 1
-          for (uint32_t u = 0;; u++) {
-            if (W.probe(ya) && aa) ML.push(ya, sa, s);
-            if (W.probe(yb) && ab) ML.push(yb, sb, s);
-            if (u + 1 >= spl) break;
-            ya = shoup_mul(ya, Gw, Gq, p);
-            yb = shoup_mul(yb, Gw, Gq, p);
-            s += 32;
-          }
-        }
-      }
-      __syncwarp();
-
-      // Tag matches: recompute the baby steps and compare full 64-bit values.
-      const uint32_t mc = *ML.count;
-      if (mc > (uint32_t)kMatchCap) {
-        if (lane == 0) {
-          const uint32_t r = atomicAdd(cb.redo_count, 1u);
-          if (r < cb.cap) cb.redo[r] = i;
-        }
-      } else if (mc > 0) {
-        uint64_t va = Bl, vb = Blb;
-#pragma unroll 1
-        for (uint32_t t = 0; t < CL; t++) {
-#pragma unroll 1
-          for (uint32_t h = 0; h < 2; h++) {
-            const uint64_t v = h ? vb : va;
-            if (t < (h ? nb : na)) {
-#pragma unroll 1
-              for (uint32_t q = 0; q < mc; q++) {
-                const Match mt = ML.list[q];
-                if (mt.y == v) {
-                  uint32_t row;
-                  if constexpr (RM == kRowsMask) {
-                    row = nth_row(cur[kElV], mt.slot);
-                  } else {
-                    const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
-                    row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
-                  }
-                  record_hit(J, hb, p, row, mt.s, (h ? jb0 : ja0) + t);
-                }
-              }
-            }
-          }
-          va = shoup_mul(va, Stw, Stq, p);
-          vb = shoup_mul(vb, Stw, Stq, p);
-        }
-      }
-    }
+    if (nact != 0) bsgs_prime<TL, RM>(J, cb, hb, W, ML, vbuf, cur, i, nact, Bl, Glm, lane, c_lo, c_hi, npaired);
     __syncwarp();
   }
   stage_wait_all();
   if (lane == 0 && npaired) atomicAdd(&hb.stat[kStatPaired], (unsigned long long)npaired);
+}
+
+// The warp-per-prime BSGS over many jobs in one persistent launch (the batched
+// form): the primes of every item's chunk form one index space, and each warp
+// walks it with the grid stride, so the work of small and large jobs spreads
+// over the whole GPU in one launch instead of one launch per job.  Every item
+// has its own constants (JobDev, read from global memory), records, hit buffers
+// and baby-step product; all items share the template's giant lanes TL and
+// start-value form RM.  Per-warp shared memory, in fixed places whatever the
+// item:
+//   [2 stages x stage_max x 8 B][kMaskRows V x 8 B][kMatchCap matches][count, 16 B]
+//   [the item's table: NB buckets x 16 B, NB counts x 4 B]
+// The record of the warp's next prime (possibly another item's) is staged by
+// cp.async while the current one runs, as in bsgs_kernel.
+template <int TL, int RM>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+bsgs_batch_kernel(const BatchItem *__restrict__ items, uint32_t nitems, uint32_t warp_bytes, uint32_t stage_max) {
+  extern __shared__ uint4 smem4[];
+  __shared__ uint32_t start[kBatchMaxItems + 1];  // prefix sums of the items' prime counts
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (uint32_t k = 0; k < nitems; k++) {
+      start[k] = acc;
+      const uint32_t c = *items[k].cb.count, cap = items[k].cb.cap;
+      acc += c < cap ? c : cap;
+    }
+    start[nitems] = acc;
+  }
+  __syncthreads();
+  const uint32_t total = start[nitems];
+  uint8_t *base = reinterpret_cast<uint8_t *>(smem4) + (size_t)warp * warp_bytes;
+  uint64_t *stage0 = reinterpret_cast<uint64_t *>(base);
+  uint64_t *vbuf = stage0 + 2 * stage_max;
+  MatchList ML;
+  ML.list = reinterpret_cast<Match *>(vbuf + kMaskRows);
+  ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
+  ML.cap = kMatchCap;
+  uint8_t *tbase = reinterpret_cast<uint8_t *>(ML.count) + 16;
+  const uint32_t nwarps = gridDim.x * kWarpsPerBlock;
+  const uint32_t first = blockIdx.x * kWarpsPerBlock + warp;
+  // the item of global index g, from the item of an earlier (smaller) index
+  auto locate = [&](uint32_t g, uint32_t k) {
+    while (k + 1 < nitems && g >= start[k + 1]) k++;
+    return k;
+  };
+
+  uint64_t nBl = 0, nGl = 0;
+  uint32_t nk = 0;               // item of the staged next prime
+  uint32_t ck = 0xffffffffu;     // item whose row constants the lanes hold
+  uint32_t c_lo = 0, c_hi = 0;
+  uint32_t npaired = 0;          // paired primes of item ck not yet added to its counter
+  auto prefetch = [&](uint32_t g, uint64_t *dst) {
+    nk = locate(g, nk);
+    const BatchItem &X = items[nk];
+    const uint32_t i = g - start[nk];
+    stage_copy(dst, X.J, X.cb, i, X.J.stage_elems, lane);
+    const uint64_t *lt = X.cb.recs + (size_t)i * X.J.rec_elems + X.J.el_tab + lane;
+    nBl = __ldg(lt);
+    nGl = __ldg(lt + 32);
+  };
+  if (first < total) prefetch(first, stage0);
+  else stage_commit_empty();
+
+#pragma unroll 1
+  for (uint32_t it = 0;; it++) {
+    const uint32_t g = first + it * nwarps;
+    if (g >= total) break;
+    const uint32_t k = nk;
+    const uint32_t i = g - start[k];
+    const uint64_t *cur = stage0 + (it & 1) * stage_max;
+    uint64_t *nxt = stage0 + ((it + 1) & 1) * stage_max;
+    const uint64_t Bl = nBl, Glm = nGl;
+    if (g + nwarps < total) prefetch(g + nwarps, nxt);
+    else stage_commit_empty();
+    const BatchItem &X = items[k];
+    if (k != ck) {
+      if (lane == 0 && npaired) atomicAdd(&items[ck].hb.stat[kStatPaired], (unsigned long long)npaired);
+      npaired = 0;
+      ck = k;
+      if constexpr (RM == kRowsMask) {
+        c_lo = lane < X.J.nrows ? __ldg(X.J.row_c + lane) : 0u;
+        c_hi = lane + 32 < X.J.nrows ? __ldg(X.J.row_c + lane + 32) : 0u;
+      }
+    }
+    stage_wait_prev();
+    __syncwarp();
+    const uint32_t nact = (uint32_t)cur[kElNact];
+    if (nact != 0) {
+      const uint32_t NB = 1u << X.J.table_log2;
+      WarpTable W;
+      W.tab4 = reinterpret_cast<uint4 *>(tbase);
+      W.tab16 = reinterpret_cast<uint16_t *>(tbase);
+      W.cnt32 = reinterpret_cast<uint32_t *>(tbase + NB * 16);
+      W.nb = NB;
+      W.bmask = NB - 1;
+      bsgs_prime<TL, RM>(X.J, X.cb, X.hb, W, ML, vbuf, cur, i, nact, Bl, Glm, lane, c_lo, c_hi, npaired);
+    }
+    __syncwarp();
+  }
+  stage_wait_all();
+  if (lane == 0 && npaired && ck < nitems) atomicAdd(&items[ck].hb.stat[kStatPaired], (unsigned long long)npaired);
+}
+
+typedef void (*BatchFn)(const BatchItem *, uint32_t, uint32_t, uint32_t);
+
+template <int RM>
+static BatchFn batch_fn_t(uint32_t tlanes) {
+  switch (tlanes) {
+    case 1: return bsgs_batch_kernel<1, RM>;
+    case 2: return bsgs_batch_kernel<2, RM>;
+    case 4: return bsgs_batch_kernel<4, RM>;
+    case 8: return bsgs_batch_kernel<8, RM>;
+    case 16: return bsgs_batch_kernel<16, RM>;
+    default: return bsgs_batch_kernel<32, RM>;
+  }
 }
 
 typedef void (*BsgsFn)(JobDev, ChunkBufs, HitBufs);
@@ -1469,6 +1599,33 @@ cudaError_t launch_bsgs(const JobDev &job, const ChunkBufs &cb, const HitBufs &h
     bsgs_cta_fn(job)<<<grid, 32 * kCtaWarps, bsgs_smem_bytes(job), st>>>(job, cb, hb);
   else
     bsgs_fn(job)<<<grid, 32 * kWarpsPerBlock, bsgs_smem_bytes(job), st>>>(job, cb, hb);
+  return cudaGetLastError();
+}
+
+static BatchFn batch_fn(const JobDev &rep) {
+  switch (row_mode(rep)) {
+    case kRowsMask: return batch_fn_t<kRowsMask>(rep.tlanes);
+    case kRowsIntId: return batch_fn_t<kRowsIntId>(rep.tlanes);
+    case kRowsIntV: return batch_fn_t<kRowsIntV>(rep.tlanes);
+    default: return batch_fn_t<kRowsV>(rep.tlanes);
+  }
+}
+
+uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max) {
+  const uint32_t b = 16 * stage_max + 8 * kMaskRows + 16 * kMatchCap + 16 + (20u << table_log2_max);
+  return (b + 15) & ~15u;
+}
+
+cudaError_t batch_configure(const JobDev &rep, uint32_t warp_bytes, int device, int *grid_out) {
+  return configure_one((const void *)batch_fn(rep), kWarpsPerBlock * (int)warp_bytes, 32 * kWarpsPerBlock, device,
+                       grid_out);
+}
+
+cudaError_t launch_bsgs_batch(const JobDev &rep, const BatchItem *items, uint32_t nitems, uint32_t stage_max,
+                              uint32_t warp_bytes, int grid, cudaStream_t st) {
+  if (nitems == 0) return cudaSuccess;
+  if (nitems > kBatchMaxItems) return cudaErrorInvalidValue;
+  batch_fn(rep)<<<grid, 32 * kWarpsPerBlock, kWarpsPerBlock * warp_bytes, st>>>(items, nitems, warp_bytes, stage_max);
   return cudaGetLastError();
 }
 

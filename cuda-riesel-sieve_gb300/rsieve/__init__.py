@@ -42,6 +42,7 @@ EXPORTS = (
     "rs_bench_imad", "rs_gpu_arith_check", "rs_last_error", "rs_version", "rs_gpu_primes_static",
     "rs_abcd_remove", "rs_server_options_default", "rs_server_create", "rs_server_submit",
     "rs_server_wait", "rs_server_destroy", "rs_job_autotune", "rs_gpu_modmul_check", "rs_bench_products",
+    "rs_batch_create", "rs_batch_add", "rs_batch_run", "rs_batch_result", "rs_batch_destroy",
 )
 
 
@@ -175,6 +176,11 @@ def lib():
         L.rs_gpu_arith_check.argtypes = [vp, vp, vp, sz, vp, vp, ctypes.c_int]
         L.rs_gpu_modmul_check.argtypes = [i32, vp, vp, vp, vp, sz, vp, ctypes.c_int]
         L.rs_bench_products.argtypes = [ctypes.c_int, vp]
+        L.rs_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        L.rs_batch_add.argtypes = [vp, vp, u64, u64, ctypes.POINTER(u32)]
+        L.rs_batch_run.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.rs_batch_result.argtypes = [vp, u32, vp, sz, ctypes.POINTER(sz), ctypes.POINTER(Stats)]
+        L.rs_batch_destroy.argtypes = [vp]
         L.rs_gpu_primes_static.argtypes = [u64, u64, vp, vp, u32, vp, u32, vp, vp]
         L.rs_abcd_remove.argtypes = [ctypes.c_char_p, sz, vp, sz, u64, vp, sz, ctypes.POINTER(sz)]
         L.rs_job_autotune.argtypes = [vp, u64, u64, u32, ctypes.POINTER(JobInfo)]
@@ -271,6 +277,58 @@ class Job:
     def close(self) -> None:
         if self._h:
             lib().rs_job_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """The batched form (rs_batch_*): many jobs' ranges sieved together, one
+    persistent BSGS launch per kernel variant per round, rounds as CUDA graphs."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p(None)
+        self._jobs = []  # keeps the added jobs alive
+        _check(lib().rs_batch_create(device, ctypes.byref(self._h)))
+
+    def add(self, job: "Job", p0: int, p1: int) -> int:
+        item = ctypes.c_uint32(0)
+        _check(lib().rs_batch_add(self._h, job._h, p0, p1, ctypes.byref(item)))
+        self._jobs.append(job)
+        return item.value
+
+    def run(self) -> dict:
+        st = Stats()
+        _check(lib().rs_batch_run(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def result(self, item: int):
+        """(factors, stats dict) of one item after run()."""
+        cap = 1 << 12
+        while True:
+            out = np.zeros(cap, dtype=FACTOR_DTYPE)
+            cnt = ctypes.c_size_t(0)
+            st = Stats()
+            rc = lib().rs_batch_result(self._h, item, out.ctypes.data, cap, ctypes.byref(cnt), ctypes.byref(st))
+            if rc == RS_ERR_CAPACITY:
+                cap = cnt.value
+                continue
+            _check(rc)
+            return out[: cnt.value], st.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            lib().rs_batch_destroy(self._h)
             self._h = ctypes.c_void_p(None)
 
     def __enter__(self):

@@ -263,6 +263,34 @@ const char *rs_last_error(void);
 const char *rs_version(void);
 
 /* ------------------------------------------------------------------------
+ * Batched form (no counterpart in the reference, which runs one job per
+ * process): the p-ranges of many created jobs sieved together, round by round.
+ * A round sieves and sets up every job's next chunk of primes, then runs the
+ * BSGS of all warp-per-prime jobs that share a kernel variant (giant lanes and
+ * start-value form) in ONE persistent launch over all their primes, so that
+ * small jobs do not leave the GPU idle; jobs of the CTA-per-prime layout run
+ * their own launch in the same round.  Each round is recorded as a CUDA graph
+ * and launched as one (the graph instantiated for a round is updated in place
+ * for the next when its shape allows).  A job of several (base, sign) parts is
+ * sieved after the rounds through its own rs_sieve_range path.  Every item's
+ * factors equal those of rs_sieve_range on the same job and range.  A job may
+ * be in one item of a batch at a time; the jobs stay the caller's.
+ * ------------------------------------------------------------------------ */
+typedef struct rs_batch rs_batch;
+
+int rs_batch_create(int device, rs_batch **batch);
+/* Add job's range [p0, p1]; *item (may be NULL) numbers it for rs_batch_result. */
+int rs_batch_add(rs_batch *batch, rs_job *job, uint64_t p0, uint64_t p1, uint32_t *item);
+/* Sieve every item.  stats (may be NULL) receives the whole run: gpu_ms from the
+ * first round to the last verification, launches, primes and factors summed. */
+int rs_batch_run(rs_batch *batch, rs_stats *stats);
+/* An item's factors (sorted by (p, k, n, b, c)) and counters after rs_batch_run;
+ * RS_ERR_CAPACITY with *count = the number found when cap is too small. */
+int rs_batch_result(const rs_batch *batch, uint32_t item, rs_factor *out, size_t cap, size_t *count,
+                    rs_stats *stats);
+int rs_batch_destroy(rs_batch *batch);
+
+/* ------------------------------------------------------------------------
  * Serving (no counterpart in the reference, which runs one job per process).
  * A server owns a device and runs submitted jobs concurrently on `slots`
  * worker threads.  Admission is by device memory: at submit a job's footprint
