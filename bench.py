@@ -293,7 +293,9 @@ def run_served(args) -> None:
     every part of a job on the same job object), batched (all requests
     submitted to an rs_server at once) and served (Poisson arrivals at a sweep
     of loads relative to the batched capacity, repeated --served-repeats
-    times).  Every request's factors in the batched and served runs are
+    times).  Beside them, the persistent batched launch (rs_batch: every job's
+    whole window in one batch, one BSGS launch per kernel variant per round).
+    Every request's factors in the batched, persistent and served runs are
     checked equal to the plain run.  Latencies are the server's own
     submit-to-finish times.
     """
