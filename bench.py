@@ -382,7 +382,7 @@ def run_served(args) -> None:
     # the persistent batched launch (rs_batch): every job's whole window in one
     # batch, one BSGS launch per kernel variant per round, rounds as CUDA graphs
     t0 = time.perf_counter()
-    bjobs = [rsieve.Job(abcd) for abcd, _, _ in jobs]
+    bjobs = [rsieve.Job(abcd, mem_limit=1 << 30) for abcd, _, _ in jobs]  # 1 GiB of chunk buffers each
     t_bcreate = time.perf_counter() - t0
     with rsieve.Batch() as bt:
         for j, (_, p0, p1) in zip(bjobs, jobs):

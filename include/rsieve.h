@@ -274,7 +274,9 @@ const char *rs_version(void);
  * for the next when its shape allows).  A job of several (base, sign) parts is
  * sieved after the rounds through its own rs_sieve_range path.  Every item's
  * factors equal those of rs_sieve_range on the same job and range.  A job may
- * be in one item of a batch at a time; the jobs stay the caller's.
+ * be in one item of a batch at a time; the jobs stay the caller's, and each
+ * holds its own chunk buffers (sized by its rs_options.mem_limit) while the
+ * batch runs, so many jobs in one batch want a modest mem_limit each.
  * ------------------------------------------------------------------------ */
 typedef struct rs_batch rs_batch;
 

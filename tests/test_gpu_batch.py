@@ -43,7 +43,7 @@ def test_batch_matches_standalone(rs, sr745_text):
         with rs.Job(text, **opts) as j:
             f, st = j.sieve(p0, p1)
         want.append((_key(f), st["primes"]))
-    jobs = [rs.Job(text, **opts) for text, opts, _, _ in specs]
+    jobs = [rs.Job(text, mem_limit=256 << 20, **opts) for text, opts, _, _ in specs]
     with rs.Batch() as bt:
         items = [bt.add(j, p0, p1) for j, (_, _, p0, p1) in zip(jobs, specs)]
         tot = bt.run()
