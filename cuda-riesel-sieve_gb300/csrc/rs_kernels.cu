@@ -1539,6 +1539,10 @@ static cudaError_t configure_one(const void *fn, int smem, int threads, int devi
   int max_smem = 0;
   cudaError_t e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, fn);
+  if (e != cudaSuccess) return e;
+  max_smem -= (int)fa.sharedSizeBytes;  // the kernel's static shared memory counts against the same limit
   if (smem > max_smem) return cudaErrorInvalidValue;
   e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
   if (e != cudaSuccess) return e;
