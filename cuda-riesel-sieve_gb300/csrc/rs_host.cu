@@ -1665,9 +1665,16 @@ extern "C" int rs_job_autotune(rs_job *j, uint64_t p0, uint64_t p1, uint32_t can
 // Batched form: many jobs' ranges in rounds, one persistent BSGS launch per
 // kernel variant per round, each round recorded as a CUDA graph.
 
+// Branches of a round's graph: the jobs' sieve and setup launches, then the
+// kernel variants' BSGS launches, are spread over this many captured streams so
+// that the graph runs them side by side.
+constexpr int kBatchBranches = 8;
+
 struct rs_batch {
   int device = 0;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;               // the captured origin stream
+  cudaStream_t side[kBatchBranches] = {};  // branch streams (forked from st in each capture)
+  cudaEvent_t fork[2] = {}, join[2][kBatchBranches] = {};
   struct Item {
     rs_job *job = nullptr;
     uint64_t p0 = 0, p1 = 0;
@@ -1687,10 +1694,16 @@ extern "C" int rs_batch_create(int device, rs_batch **out) {
   if (rc) return rc;
   rs_batch *b = new rs_batch();
   b->device = device;
-  const cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  for (int s = 0; s < kBatchBranches && e == cudaSuccess; s++) e = cudaStreamCreateWithFlags(&b->side[s], cudaStreamNonBlocking);
+  for (int h = 0; h < 2 && e == cudaSuccess; h++) {
+    e = cudaEventCreateWithFlags(&b->fork[h], cudaEventDisableTiming);
+    for (int s = 0; s < kBatchBranches && e == cudaSuccess; s++)
+      e = cudaEventCreateWithFlags(&b->join[h][s], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
-    delete b;
-    return fail(RS_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    rs_batch_destroy(b);
+    return fail(RS_ERR_CUDA, "rs_batch_create: %s", cudaGetErrorString(e));
   }
   *out = b;
   return RS_OK;
@@ -1862,44 +1875,73 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
     cudaMemsetAsync(R.pt->hb.stat, 0, kStatCount * sizeof(unsigned long long), B->st);
   }
   cudaEventRecord(ev0, B->st);
-  // the rounds, each recorded on the batch stream and launched as one graph
+  // the rounds, each recorded as one graph of two forked phases: every job's
+  // sieve and setup (jobs spread over the branch streams), then every kernel
+  // variant's persistent BSGS launch followed by its jobs' exact-path launches,
+  // and every CTA-layout job's own BSGS and exact launches (again spread over
+  // the branches).  Each job's launches stay in order on one branch; the
+  // branches run side by side.
+  auto fork = [&](int h) {
+    cudaEventRecord(B->fork[h], B->st);
+    for (int s = 0; s < kBatchBranches; s++) cudaStreamWaitEvent(B->side[s], B->fork[h], 0);
+  };
+  auto join = [&](int h) {
+    for (int s = 0; s < kBatchBranches; s++) {
+      cudaEventRecord(B->join[h][s], B->side[s]);
+      cudaStreamWaitEvent(B->st, B->join[h][s], 0);
+    }
+  };
   cudaError_t e = cudaSuccess;
   for (size_t rd = 0; rd < rounds && e == cudaSuccess; rd++) {
     e = cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) break;
+    fork(0);
+    size_t br = 0;
     for (Run &R : runs) {
       if (rd >= R.chunks.size()) continue;
+      const cudaStream_t s = B->side[br++ % kBatchBranches];
       rs_job *j = R.j;
       const Chunk &c = R.chunks[rd];
-      cudaMemsetAsync(j->cb.count, 0, 4, B->st);
+      cudaMemsetAsync(j->cb.count, 0, 4, s);
       launch_sieve(c.a, c.b, j->d_sp, j->d_sp_rcp, j->nsp, j->nsp_small, j->d_gbits, j->cb.primes, j->cb.count,
-                   j->cb.cap, B->st);
-      cudaMemcpyAsync(&h_counts[R.count0 + rd], j->cb.count, 4, cudaMemcpyDeviceToHost, B->st);
+                   j->cb.cap, s);
+      cudaMemcpyAsync(&h_counts[R.count0 + rd], j->cb.count, 4, cudaMemcpyDeviceToHost, s);
       ChunkBufs cb = j->cb;
       cb.small_step = R.forms[rd];
-      launch_setup(R.pt->dev, cb, B->st);
-      cudaMemsetAsync(j->cb.redo_count, 0, 4, B->st);
+      launch_setup(R.pt->dev, cb, s);
+      cudaMemsetAsync(j->cb.redo_count, 0, 4, s);
       tot.launches += (j->nsp > j->nsp_small ? 2 : 1) + 1;
     }
+    join(0);
+    fork(1);
+    br = 0;
     for (size_t g = 0; g < groups.size(); g++) {
       if (!gn[rd][g]) continue;
+      const cudaStream_t s = B->side[br++ % kBatchBranches];
       launch_bsgs_batch(runs[groups[g].runs[0]].pt->dev, d_items + goff[rd][g], gn[rd][g], groups[g].stage_max,
-                        groups[g].warp_bytes, groups[g].grid, B->st);
+                        groups[g].warp_bytes, groups[g].grid, s);
       tot.launches++;
       tot.bsgs_launches++;
+      for (size_t r : groups[g].runs) {
+        Run &R = runs[r];
+        if (rd >= R.chunks.size()) continue;
+        ChunkBufs cb = R.j->cb;
+        cb.small_step = R.forms[rd];
+        launch_bsgs_exact(R.pt->dev, cb, R.pt->hb, R.pt->exact_grid, s);
+        tot.launches++;
+      }
     }
     for (Run &R : runs) {
-      if (rd >= R.chunks.size()) continue;
+      if (rd >= R.chunks.size() || R.pt->dev.cta_warps <= 1) continue;
+      const cudaStream_t s = B->side[br++ % kBatchBranches];
       ChunkBufs cb = R.j->cb;
       cb.small_step = R.forms[rd];
-      if (R.pt->dev.cta_warps > 1) {
-        launch_bsgs(R.pt->dev, cb, R.pt->hb, R.pt->bsgs_grid, B->st);
-        tot.launches++;
-        tot.bsgs_launches++;
-      }
-      launch_bsgs_exact(R.pt->dev, cb, R.pt->hb, R.pt->exact_grid, B->st);
-      tot.launches++;
+      launch_bsgs(R.pt->dev, cb, R.pt->hb, R.pt->bsgs_grid, s);
+      launch_bsgs_exact(R.pt->dev, cb, R.pt->hb, R.pt->exact_grid, s);
+      tot.launches += 2;
+      tot.bsgs_launches++;
     }
+    join(1);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(B->st, &graph);
     if (e != cudaSuccess) break;
@@ -2081,6 +2123,13 @@ extern "C" int rs_batch_destroy(rs_batch *B) {
   if (B->st) {
     cudaStreamSynchronize(B->st);
     cudaStreamDestroy(B->st);
+  }
+  for (int s = 0; s < kBatchBranches; s++)
+    if (B->side[s]) cudaStreamDestroy(B->side[s]);
+  for (int h = 0; h < 2; h++) {
+    if (B->fork[h]) cudaEventDestroy(B->fork[h]);
+    for (int s = 0; s < kBatchBranches; s++)
+      if (B->join[h][s]) cudaEventDestroy(B->join[h][s]);
   }
   delete B;
   return RS_OK;
