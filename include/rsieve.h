@@ -270,8 +270,9 @@ const char *rs_version(void);
  * start-value form) in ONE persistent launch over all their primes, so that
  * small jobs do not leave the GPU idle; jobs of the CTA-per-prime layout run
  * their own launch in the same round.  Each round is recorded as a CUDA graph
- * and launched as one (the graph instantiated for a round is updated in place
- * for the next when its shape allows).  A job of several (base, sign) parts is
+ * and launched as one: the jobs' sieve and setup launches, and then the BSGS
+ * launches, sit on parallel branches of the graph (the graph instantiated for a
+ * round is updated in place for the next when its shape allows).  A job of several (base, sign) parts is
  * sieved after the rounds through its own rs_sieve_range path.  Every item's
  * factors equal those of rs_sieve_range on the same job and range.  A job may
  * be in one item of a batch at a time; the jobs stay the caller's, and each
