@@ -1752,6 +1752,7 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
     std::vector<Chunk> chunks;
     std::vector<uint32_t> forms;
     size_t count0 = 0;  // first slot of its chunks in the pinned count array
+    bool own = false;   // BSGS through the job's own launch (CTA layout, or no batch kernel fits)
   };
   std::vector<Run> runs;
   std::vector<size_t> alone;  // items sieved through their own path (several parts)
@@ -1799,25 +1800,41 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
   }
   size_t rounds = 0;
   for (Run &r : runs) rounds = std::max(rounds, r.chunks.size());
-  // groups of warp-per-prime runs sharing a kernel variant, and their launch shape
+  // groups of warp-per-prime runs sharing a kernel variant and a table size (the
+  // per-warp shared memory of a launch is sized for its largest table), and
+  // their launch shape; a group whose shape fits no launch runs its jobs' own
+  // launches, as CTA-layout jobs do
   struct Group {
-    uint32_t variant;
+    uint32_t variant, table_log2;
     std::vector<size_t> runs;
-    uint32_t stage_max = 0, tl_max = 0, warp_bytes = 0;
+    uint32_t stage_max = 0, warp_bytes = 0;
     int grid = 0;
   };
   std::vector<Group> groups;
   for (size_t r = 0; r < runs.size(); r++) {
     const JobDev &d = runs[r].pt->dev;
-    if (d.cta_warps > 1) continue;
+    if (d.cta_warps > 1) {
+      runs[r].own = true;
+      continue;
+    }
     const uint32_t v = batch_variant(d);
     size_t g = 0;
-    for (; g < groups.size() && groups[g].variant != v; g++) {
+    for (; g < groups.size() && (groups[g].variant != v || groups[g].table_log2 != d.table_log2); g++) {
     }
-    if (g == groups.size()) groups.push_back(Group{v, {}});
+    if (g == groups.size()) groups.push_back(Group{v, d.table_log2, {}});
     groups[g].runs.push_back(r);
     groups[g].stage_max = std::max(groups[g].stage_max, d.stage_elems);
-    groups[g].tl_max = std::max(groups[g].tl_max, d.table_log2);
+  }
+  for (size_t g = 0; g < groups.size();) {
+    Group &G = groups[g];
+    G.warp_bytes = batch_warp_bytes(G.stage_max, G.table_log2, runs[G.runs[0]].pt->dev.row_mask != 0);
+    if (batch_configure(runs[G.runs[0]].pt->dev, G.warp_bytes, B->device, &G.grid) == cudaSuccess) {
+      g++;
+      continue;
+    }
+    cudaGetLastError();
+    for (size_t r : G.runs) runs[r].own = true;
+    groups.erase(groups.begin() + (std::ptrdiff_t)g);
   }
   // the launch items of every (round, group), written once and copied to the device once
   std::vector<std::vector<size_t>> goff(rounds, std::vector<size_t>(groups.size(), 0));
@@ -1840,10 +1857,6 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
       if (gn[rd][g] > kBatchMaxItems) return fail(RS_ERR_INVALID, "rs_batch_run: more than %u jobs of one kernel variant",
                                                   kBatchMaxItems);
     }
-  for (Group &g : groups) {
-    g.warp_bytes = batch_warp_bytes(g.stage_max, g.tl_max);
-    CUDA_TRY(batch_configure(runs[g.runs[0]].pt->dev, g.warp_bytes, B->device, &g.grid));
-  }
   BatchItem *d_items = nullptr;
   uint32_t *h_counts = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1932,7 +1945,7 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
       }
     }
     for (Run &R : runs) {
-      if (rd >= R.chunks.size() || R.pt->dev.cta_warps <= 1) continue;
+      if (rd >= R.chunks.size() || !R.own) continue;
       const cudaStream_t s = B->side[br++ % kBatchBranches];
       ChunkBufs cb = R.j->cb;
       cb.small_step = R.forms[rd];

@@ -197,8 +197,9 @@ uint64_t bsgs_exact_scratch_bytes(const JobDev &job, int exact_grid);
 cudaError_t bsgs_configure(const JobDev &job, int device, int *grid_out, int *exact_grid_out);
 // Multi-job launch over `nitems` items in device memory that share rep's kernel
 // variant (rep: any of them); stage_max and table_log2_max are the largest over
-// the items.  batch_configure gives its per-warp shared memory and grid.
-uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max);
+// the items; row_mask: the variant builds V from an active-row mask.
+// batch_configure gives its per-warp shared memory and grid.
+uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max, bool row_mask);
 cudaError_t batch_configure(const JobDev &rep, uint32_t warp_bytes, int device, int *grid_out);
 cudaError_t launch_bsgs_batch(const JobDev &rep, const BatchItem *items, uint32_t nitems, uint32_t stage_max,
                               uint32_t warp_bytes, int grid, cudaStream_t st);

@@ -1082,7 +1082,7 @@ bsgs_kernel(JobDev J, ChunkBufs cb, HitBufs hb) {
 // and baby-step product; all items share the template's giant lanes TL and
 // start-value form RM.  Per-warp shared memory, in fixed places whatever the
 // item:
-//   [2 stages x stage_max x 8 B][kMaskRows V x 8 B][kMatchCap matches][count, 16 B]
+//   [2 stages x stage_max x 8 B]([kMaskRows V x 8 B], RM = kRowsMask)[kMatchCap matches][count, 16 B]
 //   [the item's table: NB buckets x 16 B, NB counts x 4 B]
 // The record of the warp's next prime (possibly another item's) is staged by
 // cp.async while the current one runs, as in bsgs_kernel.
@@ -1107,7 +1107,7 @@ bsgs_batch_kernel(const BatchItem *__restrict__ items, uint32_t nitems, uint32_t
   uint64_t *stage0 = reinterpret_cast<uint64_t *>(base);
   uint64_t *vbuf = stage0 + 2 * stage_max;
   MatchList ML;
-  ML.list = reinterpret_cast<Match *>(vbuf + kMaskRows);
+  ML.list = reinterpret_cast<Match *>(vbuf + (RM == kRowsMask ? kMaskRows : 0));
   ML.count = reinterpret_cast<uint32_t *>(ML.list + kMatchCap);
   ML.cap = kMatchCap;
   uint8_t *tbase = reinterpret_cast<uint8_t *>(ML.count) + 16;
@@ -1615,8 +1615,8 @@ static BatchFn batch_fn(const JobDev &rep) {
   }
 }
 
-uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max) {
-  const uint32_t b = 16 * stage_max + 8 * kMaskRows + 16 * kMatchCap + 16 + (20u << table_log2_max);
+uint32_t batch_warp_bytes(uint32_t stage_max, uint32_t table_log2_max, bool row_mask) {
+  const uint32_t b = 16 * stage_max + (row_mask ? 8 * kMaskRows : 0) + 16 * kMatchCap + 16 + (20u << table_log2_max);
   return (b + 15) & ~15u;
 }
 
