@@ -294,7 +294,8 @@ def run_served(args) -> None:
     submitted to an rs_server at once) and served (Poisson arrivals at a sweep
     of loads relative to the batched capacity, repeated --served-repeats
     times).  Beside them, the persistent batched launch (rs_batch: every job's
-    whole window in one batch, one BSGS launch per kernel variant per round).
+    whole window in one batch, one BSGS launch per kernel variant per round),
+    and plain once more at the persistent run's chunk budget (1 GiB a job).
     Every request's factors in the batched, persistent and served runs are
     checked equal to the plain run.  Latencies are the server's own
     submit-to-finish times.
@@ -397,6 +398,14 @@ def run_served(args) -> None:
     t_persist = time.perf_counter() - t0
     for j in bjobs:
         j.close()
+    # plain again at the persistent run's chunk budget (1 GiB a job): the same
+    # chunks, one job's launches after another
+    t0 = time.perf_counter()
+    gpu_plain_1g = 0.0
+    for abcd, p0, p1 in jobs:
+        with rsieve.Job(abcd, mem_limit=1 << 30) as j:
+            gpu_plain_1g += j.sieve(p0, p1)[1]["gpu_ms"] / 1e3
+    t_plain_1g = time.perf_counter() - t0
 
     reps, t_batch, ok_batch = run_server(None)
     capacity = len(reqs) / t_batch  # requests per second
@@ -426,7 +435,11 @@ def run_served(args) -> None:
         "plain": {"p_per_s": total_width / t_plain, "wall_s": t_plain, "create_s": t_create, "gpu_s": gpu_plain},
         "persistent": {"p_per_s": total_width / t_persist, "wall_s": t_persist, "vs_plain": t_plain / t_persist,
                        "create_s": t_bcreate, "gpu_s": bst["gpu_ms"] / 1e3, "bsgs_launches": bst["bsgs_launches"],
-                       "results_match_plain": bool(ok_persist)},
+                       "results_match_plain": bool(ok_persist),
+                       # one job after another at the same 1 GiB chunk budget
+                       "plain_same_budget": {"wall_s": t_plain_1g, "gpu_s": gpu_plain_1g,
+                                             "vs_it_wall": t_plain_1g / t_persist,
+                                             "vs_it_gpu": gpu_plain_1g / (bst["gpu_ms"] / 1e3)}},
         "batched": {"p_per_s": total_width / t_batch, "wall_s": t_batch, "vs_plain": t_plain / t_batch,
                     "requests_per_s": capacity, "gpu_s": sum(r["gpu_ms"] for r in reps) / 1e3,
                     "resident_requests": int(sum(r["resident"] for r in reps))},

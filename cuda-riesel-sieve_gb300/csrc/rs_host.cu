@@ -1801,9 +1801,9 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
   size_t rounds = 0;
   for (Run &r : runs) rounds = std::max(rounds, r.chunks.size());
   // groups of warp-per-prime runs sharing a kernel variant and a table size (the
-  // per-warp shared memory of a launch is sized for its largest table), and
-  // their launch shape; a group whose shape fits no launch runs its jobs' own
-  // launches, as CTA-layout jobs do
+  // per-warp shared memory of a launch is sized for its largest table), at most
+  // kBatchMaxItems runs each, and their launch shape; a group whose shape fits
+  // no launch runs its jobs' own launches, as CTA-layout jobs do
   struct Group {
     uint32_t variant, table_log2;
     std::vector<size_t> runs;
@@ -1819,7 +1819,9 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
     }
     const uint32_t v = batch_variant(d);
     size_t g = 0;
-    for (; g < groups.size() && (groups[g].variant != v || groups[g].table_log2 != d.table_log2); g++) {
+    for (; g < groups.size() && (groups[g].variant != v || groups[g].table_log2 != d.table_log2 ||
+                                 groups[g].runs.size() >= kBatchMaxItems);
+         g++) {
     }
     if (g == groups.size()) groups.push_back(Group{v, d.table_log2, {}});
     groups[g].runs.push_back(r);

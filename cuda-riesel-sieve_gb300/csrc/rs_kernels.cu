@@ -1092,14 +1092,15 @@ bsgs_batch_kernel(const BatchItem *__restrict__ items, uint32_t nitems, uint32_t
   extern __shared__ uint4 smem4[];
   __shared__ uint32_t start[kBatchMaxItems + 1];  // prefix sums of the items' prime counts
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the items' prime counts, loaded in parallel, then their prefix sums
+  for (uint32_t k = threadIdx.x; k < nitems; k += blockDim.x) {
+    const uint32_t c = *items[k].cb.count, cap = items[k].cb.cap;
+    start[k + 1] = c < cap ? c : cap;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (uint32_t k = 0; k < nitems; k++) {
-      start[k] = acc;
-      const uint32_t c = *items[k].cb.count, cap = items[k].cb.cap;
-      acc += c < cap ? c : cap;
-    }
-    start[nitems] = acc;
+    start[0] = 0;
+    for (uint32_t k = 0; k < nitems; k++) start[k + 1] += start[k];
   }
   __syncthreads();
   const uint32_t total = start[nitems];

@@ -72,3 +72,27 @@ def test_batch_rejects_a_job_twice(rs):
         with pytest.raises(rs.RsieveError) as e:
             bt.add(j, 10**9 + 10**6, 10**9 + 2 * 10**6)
         assert e.value.code == rs.RS_ERR_INVALID
+
+
+def test_batch_more_jobs_of_one_variant_than_one_launch_takes(rs):
+    """300 jobs of one kernel variant and table size: the launch takes at most
+    256 jobs, so each round runs two; every item still equals its own run."""
+    import rsieve.synth as S
+
+    b, s, ks, nl = S.plain_job(1)
+    text = S.to_abcd(b, s, ks[:10], nl[:10])  # 44 datless factors over the 300 windows
+    n = 300
+    wins = [(2**33 + 1 + i * 40000, 2**33 + (i + 1) * 40000) for i in range(n)]
+    jobs = [rs.Job(text, mem_limit=16 << 20, datless=1) for _ in range(n)]
+    try:
+        want = [_key(j.sieve(p0, p1)[0]) for j, (p0, p1) in zip(jobs, wins)]
+        with rs.Batch() as bt:
+            items = [bt.add(j, p0, p1) for j, (p0, p1) in zip(jobs, wins)]
+            tot = bt.run()
+            for it, w in zip(items, want):
+                assert _key(bt.result(it)[0]) == w, it
+        assert sum(len(w) for w in want) > 30
+        assert tot["bsgs_launches"] >= 2
+    finally:
+        for j in jobs:
+            j.close()
