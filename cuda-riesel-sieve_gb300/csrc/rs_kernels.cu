@@ -610,7 +610,15 @@ constexpr uint32_t kSlots = 8;  // tag slots per bucket
 // the tag from the high 16 bits: the low bits masked when NB is a power of two
 // (MUL false), else scaled, (lo16 * NB) >> 16 (MUL true; any NB <= 65536), which
 // lets a CTA size its table to its shared memory instead of to a power of two.
-template <bool MUL>
+//
+// SIG: the bucket's count word also holds a 16-bit signature of its entries:
+// the count in bits 0-15 (a bucket sees at most m <= 2^15 increments, so it
+// never carries out), and bit 16 + sig(v) set (atomic OR) for every entry v
+// stored there, sig(v) a 4-bit hash of v's high word.  A tag match counts only
+// if the bucket holding the tag has the signature bit of the probed value, so
+// with ~2 entries a bucket ~88% of the false 16-bit matches are rejected
+// before they cost a pass over the baby steps; a true match always has its bit.
+template <bool MUL, bool SIG = false>
 struct TableT {
   uint4 *tab4;
   uint16_t *tab16;
@@ -624,29 +632,36 @@ struct TableT {
   __device__ __forceinline__ uint32_t next(uint32_t b) const {
     return MUL ? (b + 1 == nb ? 0u : b + 1) : ((b + 1) & bmask);
   }
+  __device__ __forceinline__ static uint32_t sig_bit(uint64_t v) {
+    return 1u << (16 + ((uint32_t)(v >> 32) * 0x9E3779B1u >> 28));
+  }
 
   __device__ __forceinline__ uint32_t take(uint32_t b) const {
-    return atomicAdd(&cnt32[b], 1u);
+    const uint32_t c = atomicAdd(&cnt32[b], 1u);
+    return SIG ? c & 0xffffu : c;
+  }
+  __device__ __forceinline__ void store(uint64_t v, uint32_t b, uint32_t c) const {
+    tab16[b * kSlots + c] = (uint16_t)tag_pair((uint32_t)v);
+    if (SIG) atomicOr(&cnt32[b], sig_bit(v));
   }
 
   // Insert continuing after bucket b, whose slots are all taken.
-  __device__ __forceinline__ void insert_after(uint32_t lo, uint32_t b) const {
+  __device__ __forceinline__ void insert_after(uint64_t v, uint32_t b) const {
     uint32_t c = kSlots;
 #pragma unroll 1
     for (uint32_t g = 0; c >= kSlots && g + 1 < nb; g++) {
       b = next(b);
       c = take(b);
     }
-    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
+    if (c < kSlots) store(v, b, c);
   }
 
   // Insert into the home bucket; false if it was full (the caller finishes the
   // insert later with insert_after, keeping the rare overflow off the hot loop).
   __device__ __forceinline__ bool insert_home(uint64_t v) const {
-    const uint32_t lo = (uint32_t)v;
-    const uint32_t b = home(lo);
+    const uint32_t b = home((uint32_t)v);
     const uint32_t c = take(b);
-    if (c < kSlots) tab16[b * kSlots + c] = (uint16_t)tag_pair(lo);
+    if (c < kSlots) store(v, b, c);
     return c < kSlots;
   }
 
@@ -660,19 +675,22 @@ struct TableT {
     return (zero_half(m) | (q.w & 0xffff0000u)) != 0;  // a tag match, or slot 7 taken
   }
 
-  // True iff some entry with the tag of y lies in y's probe sequence.
+  // True iff some entry with the tag of y (and, SIG, the signature bit of y)
+  // lies in y's probe sequence.
   __device__ __forceinline__ bool probe(uint64_t y) const {
     const uint32_t lo = (uint32_t)y;
     uint32_t b = home(lo);
     const uint32_t T = tag_pair(lo);
+    const uint32_t sb = SIG ? sig_bit(y) : 0u;
+    auto has = [&](const uint4 &q, uint32_t bk) { return bucket_has(q, T) && (!SIG || (cnt32[bk] & sb)); };
     uint4 q = tab4[b];
-    bool hit = bucket_has(q, T);
+    bool hit = has(q, b);
     if (q.w >= 0x10000u) {  // the home bucket is full, continue scanning
 #pragma unroll 1
       for (uint32_t g = 0; g + 1 < nb; g++) {
         b = next(b);
         q = tab4[b];
-        hit |= bucket_has(q, T);
+        hit |= has(q, b);
         if (q.w < 0x10000u) break;
       }
     }
@@ -875,7 +893,7 @@ __device__ __forceinline__ void bsgs_prime(const JobDev &J, const ChunkBufs &cb,
     const uint64_t v = lane < novf ? ovf[lane] : 0;
     __syncwarp();
     if (lane == 0) *ML.count = 0;
-    if (lane < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
+    if (lane < novf) W.insert_after(v, W.home((uint32_t)v));
     __syncwarp();
   }
 
@@ -1309,7 +1327,7 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t NB = J.nbuckets;
   uint8_t *base = reinterpret_cast<uint8_t *>(smem4);
-  TableT<MUL> W;
+  TableT<MUL, true> W;
   W.tab4 = reinterpret_cast<uint4 *>(base);
   W.tab16 = reinterpret_cast<uint16_t *>(base);
   W.cnt32 = reinterpret_cast<uint32_t *>(base + NB * 16);
@@ -1375,7 +1393,7 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
       const uint64_t v = tid < novf ? ovf[tid] : 0;
       __syncthreads();
       if (tid == 0) *ML.count = 0;
-      if (tid < novf) W.insert_after((uint32_t)v, W.home((uint32_t)v));
+      if (tid < novf) W.insert_after(v, W.home((uint32_t)v));
       __syncthreads();
     }
 
@@ -1404,25 +1422,37 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
         if (r < cb.cap) cb.redo[r] = i;
       }
     } else if (mc > 0) {
-      uint64_t va = Bl, vb = Blb;
-      const uint64_t Stw = rec[kElStw], Stq = rec[kElStq];
-      const uint32_t bq = J.bq_small, rcp = (uint32_t)rec[kElRcp];
-      const bool small = cb.small_step == kStepSmall;
+      // The first four matched values stay in registers (most primes have one
+      // or two false tag matches); only a step whose value equals one of them
+      // (or every step, with more than four matches) scans the list.
+      const uint64_t y0 = ML.list[0].y;
+      const uint64_t y1 = mc > 1 ? ML.list[1].y : y0;
+      const uint64_t y2 = mc > 2 ? ML.list[2].y : y0;
+      const uint64_t y3 = mc > 3 ? ML.list[3].y : y0;
+      auto pass = [&](auto step) {
+        uint64_t va = Bl, vb = Blb;
+#pragma unroll 2
+        for (uint32_t t = 0; t < CL; t++) {
+          const bool in_a = va == y0 || va == y1 || va == y2 || va == y3;
+          const bool in_b = vb == y0 || vb == y1 || vb == y2 || vb == y3;
+          if (in_a || in_b || mc > 4) {
 #pragma unroll 1
-      for (uint32_t t = 0; t < CL; t++) {
-#pragma unroll 1
-        for (uint32_t q = 0; q < mc; q++) {
-          const Match mt = ML.list[q];
-          if (mt.y == va || mt.y == vb) {  // both when B has a small order
-            const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
-            const uint32_t row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
-            if (mt.y == va) record_hit(J, hb, p, row, mt.s, ja0 + t);
-            if (mt.y == vb) record_hit(J, hb, p, row, mt.s, jb0 + t);
+            for (uint32_t q = 0; q < mc; q++) {
+              const Match mt = ML.list[q];
+              if (mt.y == va || mt.y == vb) {  // both when B has a small order
+                const uint64_t pk = rec_el(J, cb, J.el_row + (mt.slot >> 2), i);
+                const uint32_t row = (uint32_t)(pk >> (16 * (mt.slot & 3))) & 0xffffu;
+                if (mt.y == va) record_hit(J, hb, p, row, mt.s, ja0 + t);
+                if (mt.y == vb) record_hit(J, hb, p, row, mt.s, jb0 + t);
+              }
+            }
           }
+          va = step(va);
+          vb = step(vb);
         }
-        va = small ? mul_small(va, bq, rcp, p) : shoup_mul(va, Stw, Stq, p);
-        vb = small ? mul_small(vb, bq, rcp, p) : shoup_mul(vb, Stw, Stq, p);
-      }
+      };
+      if (cb.small_step == kStepSmall) pass(StepSmall{J.bq_small, (uint32_t)rec[kElRcp], p});
+      else pass(StepShoup{rec[kElStw], rec[kElStq], p});
     }
   }
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
