@@ -518,7 +518,8 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
           if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536 || 20.0 * nb_opts[0] + vbytes + 16.0 * (kCtaMatchCap + 1) <= 232448.0))
             continue;
           const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
-          if (m <= mcap && m * T >= X && slog <= 17 && smem <= 232448.0 && fp <= 16.0) {
+          // (m < 2^16: a bucket's insert count is the low half of its count word)
+          if (m <= mcap && m < 65536 && m * T >= X && slog <= 17 && smem <= 232448.0 && fp <= 16.0) {
             const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
                                  nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
                                 std::sqrt(kFullWarps / kCtaWarps) * kCtaStepCost;

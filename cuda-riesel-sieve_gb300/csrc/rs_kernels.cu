@@ -612,8 +612,9 @@ constexpr uint32_t kSlots = 8;  // tag slots per bucket
 // lets a CTA size its table to its shared memory instead of to a power of two.
 //
 // SIG: the bucket's count word also holds a 16-bit signature of its entries:
-// the count in bits 0-15 (a bucket sees at most m <= 2^15 increments, so it
-// never carries out), and bit 16 + sig(v) set (atomic OR) for every entry v
+// the count in bits 0-15 (a bucket sees at most one increment per baby step,
+// and the planner keeps CTA plans below 2^16 baby steps, so it never carries
+// out), and bit 16 + sig(v) set (atomic OR) for every entry v
 // stored there, sig(v) a 4-bit hash of v's high word.  A tag match counts only
 // if the bucket holding the tag has the signature bit of the probed value, so
 // with ~2 entries a bucket ~88% of the false 16-bit matches are rejected
@@ -1316,7 +1317,8 @@ __device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, 
 // t + 32W into one table that fills most of the SM's shared memory, and warp w
 // takes the giant steps of row slots w, w + W, ... (32 lanes per row, T/32
 // steps per lane).  Shared memory:
-//   [NB buckets x 16 B][NB counts x 4 B][V, max_act x 8 B][kCtaMatchCap matches][count, 16 B]
+//   [NB buckets x 16 B][NB count words x 4 B: insert count, entries' signature]
+//   [V, max_act x 8 B][kCtaMatchCap matches][count, 16 B]
 // V is staged with cp.async during the baby steps.  Table operations, the
 // deferred overflow inserts and the exact tag-match resolution are those of
 // bsgs_kernel; hits are pushed where they are found (tag matches are rare).
