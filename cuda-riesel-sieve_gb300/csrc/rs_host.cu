@@ -515,11 +515,11 @@ static int make_plan(const Seqs &s, const rs_options &opt, Plan &pl, bool with_b
           const uint32_t nbk = nb_opts[o];
           const double nb = (double)nbk;
           const double smem = 20.0 * nb + vbytes + 16.0 * (kCtaMatchCap + 1);
-          if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536 || 20.0 * nb_opts[0] + vbytes + 16.0 * (kCtaMatchCap + 1) <= 232448.0))
+          if (o == 1 && (nbk >= nb_opts[0] || nbk > 65536 || 20.0 * nb_opts[0] + vbytes + 16.0 * (kCtaMatchCap + 1) <= kCtaSmemMax))
             continue;
           const double fp = ER * (double)T * ((double)m / nb) / 65536.0;
           // (m < 2^16: a bucket's insert count is the low half of its count word)
-          if (m <= mcap && m < 65536 && m * T >= X && slog <= 17 && smem <= 232448.0 && fp <= 16.0) {
+          if (m <= mcap && m < 65536 && m * T >= X && slog <= 17 && smem <= kCtaSmemMax && fp <= 16.0) {
             const double cost = ((double)m / 32.0 + kGiantWeight * kCtaWarps * std::ceil(ER / kCtaWarps) * spl +
                                  nb * 8 / 1024.0 + 3.7 + kRowCost * rows + std::min(1.0, fp) * (double)m / 32.0) *
                                 std::sqrt(kFullWarps / kCtaWarps) * kCtaStepCost;
@@ -928,12 +928,20 @@ static int upload_part(rs_job *j, Part &pt) {
     d.stage_full = 0;
     d.stage_elems = d.el_v;
   }
-  if (d.cta_warps > 1)  // bytes per CTA: table, counts, V (or row ids), match list
+  d.ctab_smem = 0;
+  if (d.cta_warps > 1) {  // bytes per CTA: table, counts, V (or row ids), match list (, row table)
     d.warp_smem = (uint32_t)align_up(20u * d.nbuckets +
                                          (d.row_ids_only ? 16 * ((d.max_act + 7) / 8) : 8 * ((d.max_act + 1) & ~1u)) +
                                          kCtaMatchCap * 16 + 16,
                                      16);
-  else  // bytes per warp: table, counts, two record stages, (V of a row mask,) match list
+    // row ids: the kernel reads k*b^r of each row from a shared-memory copy of
+    // the job's row table when it fits beside the rest
+    const uint32_t ctab_bytes = (uint32_t)align_up(4ull * d.nrows, 16);
+    if (d.row_ids_only && d.warp_smem + ctab_bytes <= kCtaSmemMax) {
+      d.ctab_smem = 1;
+      d.warp_smem += ctab_bytes;
+    }
+  } else  // bytes per warp: table, counts, two record stages, (V of a row mask,) match list
     d.warp_smem = (uint32_t)align_up((20u << d.table_log2) + 16 * d.stage_elems + (d.row_mask ? 8 * kMaskRows : 0) +
                                          kMatchCap * 16 + 16,
                                      16);

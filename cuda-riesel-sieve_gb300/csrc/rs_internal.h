@@ -69,6 +69,7 @@ constexpr uint32_t kStepShoup = 0, kStepSmall = 1, kStepHigh = 2;  // ChunkBufs:
 constexpr int kRowsV = 0, kRowsIntV = 1, kRowsIntId = 2, kRowsMask = 3;
 constexpr uint32_t kMaskRows = 64;  // rows a row_mask record can describe
 constexpr int kCtaWarps = 16;      // warps sharing one prime in the CTA-per-prime kernel
+constexpr uint32_t kCtaSmemMax = 232448;  // shared memory a CTA may opt into (227 KB)
 constexpr int kCtaMatchCap = 64;   // deferred tag matches per prime there
 
 // Per-k data of the setup kernel's row loop, 32 bytes: odd part of k, its 2-adic
@@ -115,6 +116,7 @@ struct JobDev {
   uint32_t warp_smem;    // shared-memory bytes per warp (bsgs_kernel) or per CTA (bsgs_cta_kernel)
   uint32_t exact_log2;   // slots of the exact kernel's table = 1 << exact_log2
   uint32_t exact_global; // that table exceeds shared memory: it lives in ChunkBufs::exact_tab
+  uint32_t ctab_smem;    // CTA kernel, row ids: the table k*b^r of every row is copied into shared memory
   // device arrays
   const uint32_t *row_r;     // [nrows] n mod Q of each row
   const uint32_t *row_kidx;  // [nrows] index of the row's k

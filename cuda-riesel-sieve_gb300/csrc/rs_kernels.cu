@@ -1247,15 +1247,17 @@ int bsgs_smem_bytes(const JobDev &job) {
 // buckets only and records the outcome as bits (step u of slot k -> bit 4u + k,
 // spl <= 8); tag hits and full buckets are finished after each pass.  RM: vst
 // holds V (kRowsV), the integers k*b^r (kRowsIntV) or 16-bit row ids whose
-// k*b^r come from the job's table ctab (kRowsIntId).  TWO (integer rows, spl == 2): the
+// k*b^r come from the job's table ctab (kRowsIntId; CS: ctab is the CTA's
+// shared-memory copy of it).  TWO (integer rows, spl == 2): the
 // second value of a slot is also c times a lane multiplier, Z advanced by G^32
 // (Glw2, Glq2), so both products are independent short ones.
-template <int RM, bool TWO, class Table>
+template <int RM, bool TWO, bool CS, class Table>
 __device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, const uint64_t *vst, uint32_t nact,
                                            uint32_t warp, uint32_t lane, uint32_t spl, uint64_t Glw, uint64_t Glq,
                                            uint64_t Gw, uint64_t Gq, uint64_t p, const uint32_t *__restrict__ ctab,
                                            uint64_t Glw2 = 0, uint64_t Glq2 = 0) {
   const uint16_t *rid = reinterpret_cast<const uint16_t *>(vst);
+  auto row_c = [&](uint32_t r) -> uint32_t { return CS ? ctab[r] : __ldg(ctab + r); };
 #pragma unroll 1
   for (uint32_t s0 = warp; s0 < nact; s0 += 4 * kCtaWarps) {
     uint64_t y[4];
@@ -1266,7 +1268,7 @@ __device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, 
       const uint32_t sl = s0 + k * kCtaWarps;
       valid |= (sl < nact ? 0x11111111u : 0u) << k;
       if (RM == kRowsIntId) {
-        c[k] = __ldg(ctab + rid[sl < nact ? sl : s0]);
+        c[k] = row_c(rid[sl < nact ? sl : s0]);
         y[k] = shoup_mul32(c[k], Glw, Glq, p);
       } else if (RM == kRowsIntV) {
         c[k] = (uint32_t)vst[sl < nact ? sl : s0];
@@ -1301,7 +1303,7 @@ __device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, 
       const uint32_t b = __ffs(bits) - 1;
       bits &= bits - 1;
       const uint32_t k = b & 3, u = b >> 2, sl = s0 + k * kCtaWarps;
-      uint64_t v = RM == kRowsIntId  ? shoup_mul32(__ldg(ctab + rid[sl]), Glw, Glq, p)
+      uint64_t v = RM == kRowsIntId  ? shoup_mul32(row_c(rid[sl]), Glw, Glq, p)
                    : RM == kRowsIntV ? shoup_mul32((uint32_t)vst[sl], Glw, Glq, p)
                                      : shoup_mul(vst[sl], Glw, Glq, p);
 #pragma unroll 1
@@ -1318,7 +1320,8 @@ __device__ __forceinline__ void cta_giants(const Table &W, const MatchList &ML, 
 // takes the giant steps of row slots w, w + W, ... (32 lanes per row, T/32
 // steps per lane).  Shared memory:
 //   [NB buckets x 16 B][NB count words x 4 B: insert count, entries' signature]
-//   [V, max_act x 8 B][kCtaMatchCap matches][count, 16 B]
+//   [V, max_act x 8 B][kCtaMatchCap matches][count, 16 B]([row table, nrows x 4 B])
+// The row table (row ids only, when it fits) is copied once per launch.
 // V is staged with cp.async during the baby steps.  Table operations, the
 // deferred overflow inserts and the exact tag-match resolution are those of
 // bsgs_kernel; hits are pushed where they are found (tag matches are rare).
@@ -1347,6 +1350,11 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
   const uint32_t CL = J.chain_len, spl = J.steps_per_lane;
   const uint32_t ja0 = tid * CL, jb0 = (tid + G) * CL;  // the thread's chains; m == 2*G*CL
   const uint32_t vdst = (uint32_t)__cvta_generic_to_shared(vst);
+  // the row table, copied once per launch (row ids, when it fits); the first
+  // barrier of the prime loop orders these stores before any read
+  uint32_t *cts = reinterpret_cast<uint32_t *>(reinterpret_cast<uint8_t *>(ML.count) + 16);
+  if (RM == kRowsIntId && J.ctab_smem)
+    for (uint32_t r = tid; r < J.nrows; r += G) cts[r] = __ldg(J.row_c + r);
 
 #pragma unroll 1
   for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
@@ -1403,16 +1411,29 @@ __global__ void __launch_bounds__(32 * kCtaWarps, 1) bsgs_cta_kernel(JobDev J, C
     const uint64_t Glm = rec[J.el_tab + 32 + lane];
     const uint64_t Glw = from_mont(Glm, p, pinv), Glq = shoup_const(Glm, pinv);
     const uint64_t Gw = rec[kElGw], Gq = rec[kElGq];
-    if constexpr (RM != kRowsV) {
+    if constexpr (RM == kRowsIntId) {
       if (spl == 2) {
         const uint64_t E2 = shoup_mul(Glm, Gw, Gq, p);  // Z advanced by G^32, times 2^128
-        cta_giants<RM, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c,
-                               from_mont(E2, p, pinv), shoup_const(E2, pinv));
+        const uint64_t E2w = from_mont(E2, p, pinv), E2q = shoup_const(E2, pinv);
+        if (J.ctab_smem)
+          cta_giants<RM, true, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, cts, E2w, E2q);
+        else
+          cta_giants<RM, true, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c, E2w, E2q);
+      } else if (J.ctab_smem) {
+        cta_giants<RM, false, true>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, cts);
       } else {
-        cta_giants<RM, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
+        cta_giants<RM, false, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
+      }
+    } else if constexpr (RM == kRowsIntV) {
+      if (spl == 2) {
+        const uint64_t E2 = shoup_mul(Glm, Gw, Gq, p);  // Z advanced by G^32, times 2^128
+        cta_giants<RM, true, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c,
+                                    from_mont(E2, p, pinv), shoup_const(E2, pinv));
+      } else {
+        cta_giants<RM, false, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
       }
     } else {
-      cta_giants<kRowsV, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
+      cta_giants<kRowsV, false, false>(W, ML, vst, nact, warp, lane, spl, Glw, Glq, Gw, Gq, p, J.row_c);
     }
     __syncthreads();
 
