@@ -231,6 +231,11 @@ def test_plan_layouts(rs):
     # expected false tag matches per prime stay well inside the CTA match list
     er = d["rows"] * (0.5 if d["Q"] % 2 == 0 else 0.75)
     assert er * d["giant_steps"] * d["baby_steps"] / (d["table_slots"] / 8) / 65536 <= 16
+    # a CTA plan stays below 2^16 baby steps (a bucket's insert count is the low
+    # half of its count word) at the largest -m values
+    for hm in (12, 13, 14):
+        d = rs.plan_abcd(wide, hash_m=hm)
+        assert d["warps_per_prime"] == 1 or d["baby_steps"] < 65536
 
 
 def test_plan_row_forms(rs, sr745_text):
