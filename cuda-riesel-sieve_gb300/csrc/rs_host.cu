@@ -19,6 +19,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "rs_internal.h"
@@ -659,6 +660,21 @@ struct Part {
   void *d_hits = nullptr;
   int bsgs_grid = 0;
   int exact_grid = 0;
+  // Quadratic-character tables (rs_options.char_tables): the odd parts k' with
+  // a table and their word offsets in the job arrays, which of them are built,
+  // each k's table (index into tab_k, or -1) and the base's, the host copies of
+  // the per-k table offsets and records that go to the device as tables are
+  // built, and the primes the part has sieved (estimated from its ranges).
+  std::vector<uint32_t> tab_k, tab_off;
+  std::vector<uint8_t> tab_built;
+  std::vector<int32_t> ktab;
+  int32_t btab = -1;
+  std::vector<uint32_t> kjac_host;
+  std::vector<KInfo> kinfo_host;
+  const uint32_t *d_tab_k = nullptr, *d_tab_off = nullptr;
+  uint32_t *d_jac_bits = nullptr, *d_kjac = nullptr;
+  KInfo *d_kinfo = nullptr;
+  double primes_seen = 0;
 };
 
 struct rs_job {
@@ -775,6 +791,54 @@ static uint64_t part_array_bytes(const Plan &pl, const Seqs &s, bool datless) {
   return b + 20 * 256;  // section alignment
 }
 
+// Primes in [a, b], estimated (b - a + 1) / ln b.
+static double primes_estimate(uint64_t a, uint64_t b) {
+  if (b < a) return 0.0;
+  return (double)(b - a + 1) / std::log((double)std::max<uint64_t>(b, 16));
+}
+
+// Build the character tables of a part that pay for themselves: every table
+// when `all`, else those whose k' is at most the primes the part has sieved,
+// counting `primes_more` (the estimate of the range about to be sieved) -- a
+// table costs one Jacobi symbol per entry, and saves one per prime sieved.
+// The per-k table offsets on the device (and the base's, in the part's
+// JobDev) follow, on the job's stream, ahead of the setup launches.
+static int build_char_tables(rs_job *j, Part &pt, double primes_more, bool all) {
+  if (pt.tab_k.empty()) return RS_OK;
+  pt.primes_seen += primes_more;
+  std::vector<uint32_t> sel, first;
+  uint64_t words = 0;
+  for (size_t t = 0; t < pt.tab_k.size(); t++)
+    if (!pt.tab_built[t] && (all || (double)pt.tab_k[t] <= pt.primes_seen)) {
+      sel.push_back((uint32_t)t);
+      first.push_back((uint32_t)words);
+      words += (pt.tab_k[t] + 31) / 32;
+    }
+  if (sel.empty()) return RS_OK;
+  std::vector<uint32_t> args(sel);
+  args.insert(args.end(), first.begin(), first.end());
+  uint32_t *d_args = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **)&d_args, args.size() * 4, j->st));
+  cudaError_t e = cudaMemcpyAsync(d_args, args.data(), args.size() * 4, cudaMemcpyHostToDevice, j->st);
+  if (e == cudaSuccess)
+    e = launch_jacobi_tables(pt.d_tab_k, pt.d_tab_off, d_args, d_args + sel.size(), (uint32_t)sel.size(),
+                             (uint32_t)words, pt.d_jac_bits, j->st);
+  cudaFreeAsync(d_args, j->st);
+  if (e != cudaSuccess) return fail(RS_ERR_CUDA, "character tables: %s", cudaGetErrorString(e));
+  for (uint32_t t : sel) pt.tab_built[t] = 1;
+  const size_t nk = pt.ktab.size();
+  for (size_t i = 0; i < nk; i++) {
+    const int32_t t = pt.ktab[i];
+    const uint32_t off = t >= 0 && pt.tab_built[t] ? pt.tab_off[t] : kNoTable;
+    pt.kjac_host[i] = off;
+    pt.kinfo_host[i].k_jac = off;
+  }
+  if (pt.btab >= 0 && pt.tab_built[pt.btab]) pt.dev.b_jac = pt.tab_off[pt.btab];
+  CUDA_TRY(cudaMemcpyAsync(pt.d_kjac, pt.kjac_host.data(), nk * 4, cudaMemcpyHostToDevice, j->st));
+  CUDA_TRY(cudaMemcpyAsync(pt.d_kinfo, pt.kinfo_host.data(), nk * sizeof(KInfo), cudaMemcpyHostToDevice, j->st));
+  return RS_OK;
+}
+
 static int upload_part(rs_job *j, Part &pt) {
   const Plan &pl = pt.plan;
   const Seqs &s = pt.seqs;
@@ -803,34 +867,43 @@ static int upload_part(rs_job *j, Part &pt) {
   const size_t o_rr = sec(pl.row_r.size() * 4), o_rk = sec(pl.row_kidx.size() * 4), o_rc = sec(row_c.size() * 4);
   const size_t o_kv = sec(nk * 4), o_ko = sec(nk * 4), o_ke = sec(nk * 4), o_kr = sec(nk * 8);
   const size_t o_k0 = sec((nk + 1) * 4), o_bm = sec(pl.bitmap.size() * 4);
-  // Quadratic-character tables, one per distinct odd part > 1 of k and b,
-  // built on the device when they fit in 1 GB (about 60 ms of build time).
-  std::vector<uint32_t> tab_k, tab_off;  // odd parts and their word offsets
-  std::vector<uint32_t> kjac(nk, kNoTable);
-  uint32_t bjac = kNoTable;
+  // Quadratic-character tables, one per distinct odd part > 1 of k and b, room
+  // for all of them when they fit in 1 GB; each is built on the device when it
+  // pays (build_char_tables), until then the setup kernel computes (k/p).
+  std::vector<uint32_t> &tab_k = pt.tab_k, &tab_off = pt.tab_off;  // odd parts and their word offsets
+  tab_k.clear();
+  tab_off.clear();
+  pt.ktab.assign(nk, -1);
+  pt.btab = -1;
   uint64_t twords = 0;
-  {
+  if (j->opt.char_tables != RS_TABLES_NEVER) {
     uint32_t bo = s.base;
     while (!(bo & 1)) bo >>= 1;
-    auto find_or_add = [&](uint32_t ko) -> uint32_t {
-      if (ko <= 1) return kNoTable;
-      for (size_t t = 0; t < tab_k.size(); t++)
-        if (tab_k[t] == ko) return tab_off[t];
+    std::unordered_map<uint32_t, int32_t> index;
+    auto find_or_add = [&](uint32_t ko) -> int32_t {
+      if (ko <= 1) return -1;
+      const auto f = index.find(ko);
+      if (f != index.end()) return f->second;
       tab_k.push_back(ko);
       tab_off.push_back((uint32_t)twords);
       twords += (ko + 31) / 32;
-      return tab_off.back();
+      return index[ko] = (int32_t)tab_k.size() - 1;
     };
-    for (uint32_t i = 0; i < nk; i++) kjac[i] = find_or_add(kodd[i]);
-    bjac = find_or_add(bo);
+    for (uint32_t i = 0; i < nk; i++) pt.ktab[i] = find_or_add(kodd[i]);
+    pt.btab = find_or_add(bo);
     if (twords > (256ull << 20)) {  // too large: compute the symbols instead
-      std::fill(kjac.begin(), kjac.end(), kNoTable);
-      bjac = kNoTable;
+      std::fill(pt.ktab.begin(), pt.ktab.end(), -1);
+      pt.btab = -1;
       tab_k.clear();
       tab_off.clear();
       twords = 0;
     }
   }
+  pt.tab_built.assign(tab_k.size(), 0);
+  pt.primes_seen = 0;
+  std::vector<uint32_t> &kjac = pt.kjac_host;  // no table built yet
+  kjac.assign(nk, kNoTable);
+  const uint32_t bjac = kNoTable;
   const size_t o_kj = sec(nk * 4), o_ki = sec(nk * sizeof(KInfo)), o_tk = sec(tab_k.size() * 4);
   const size_t o_to = sec(tab_off.size() * 4);
   const size_t o_jb = sec(twords * 4);
@@ -847,7 +920,8 @@ static int upload_part(rs_job *j, Part &pt) {
   memcpy(host.data() + o_bm, pl.bitmap.data(), pl.bitmap.size() * 4);
   memcpy(host.data() + o_kj, kjac.data(), nk * 4);
   {
-    std::vector<KInfo> ki(nk);
+    std::vector<KInfo> &ki = pt.kinfo_host;
+    ki.assign(nk, KInfo{});
     for (uint32_t i = 0; i < nk; i++) {
       ki[i].k_odd = kodd[i];
       ki[i].k_e2 = ke2[i];
@@ -868,9 +942,11 @@ static int upload_part(rs_job *j, Part &pt) {
   pt.dev_bytes = off;
   CUDA_TRY(cudaMemcpyAsync(pt.d_job, host.data(), o_jb, cudaMemcpyHostToDevice, j->st));
   uint8_t *b = (uint8_t *)pt.d_job;
-  CUDA_TRY(launch_jacobi_tables((const uint32_t *)(b + o_tk), (const uint32_t *)(b + o_to),
-                                (uint32_t)tab_k.size(), (uint32_t)twords, (uint32_t *)(b + o_jb), j->st));
-  CUDA_TRY(cudaStreamSynchronize(j->st));
+  pt.d_tab_k = (const uint32_t *)(b + o_tk);
+  pt.d_tab_off = (const uint32_t *)(b + o_to);
+  pt.d_jac_bits = (uint32_t *)(b + o_jb);
+  pt.d_kjac = (uint32_t *)(b + o_kj);
+  pt.d_kinfo = (KInfo *)(b + o_ki);
   JobDev &d = pt.dev;
   d.base = s.base;
   d.sign = s.sign;
@@ -966,6 +1042,11 @@ static int upload_part(rs_job *j, Part &pt) {
   d.b_odd = bb;
   d.b_e2 = be;
   d.b_rcp = bb > 1 ? (~0ull) / bb : 0;
+  if (j->opt.char_tables == RS_TABLES_ALWAYS) {
+    const int rc = build_char_tables(j, pt, 0.0, true);
+    if (rc) return rc;
+  }
+  CUDA_TRY(cudaStreamSynchronize(j->st));
   return RS_OK;
 }
 
@@ -1370,6 +1451,8 @@ static int sieve_range_impl(rs_job *j, uint64_t p0, uint64_t p1, rs_factor *out,
       rc = ensure_hit_buffers(j, *pt, P == 1 ? 1u << 20 : 1u << 16);
       if (rc) return rc;
     }
+    rc = build_char_tables(j, *pt, primes_estimate(lo, hi), false);
+    if (rc) return rc;
   }
   const uint32_t C = j->cb.cap;
 
@@ -1793,6 +1876,7 @@ extern "C" int rs_batch_run(rs_batch *B, rs_stats *stats) {
     int rc = ensure_sieving_primes(j, r.hi, &tot.h2d_bytes);
     if (!rc) rc = ensure_chunk_buffers(j, j->cb.cap);
     if (!rc && !r.pt->d_hits) rc = ensure_hit_buffers(j, *r.pt, 1u << 20);
+    if (!rc) rc = build_char_tables(j, *r.pt, primes_estimate(r.lo, r.hi), false);
     if (rc) return rc;
     r.chunks = plan_chunks(r.lo, r.hi, j->cb.cap);
     uint64_t words = 0;

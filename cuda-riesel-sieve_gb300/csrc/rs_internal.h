@@ -206,8 +206,12 @@ cudaError_t batch_configure(const JobDev &rep, uint32_t warp_bytes, int device, 
 cudaError_t launch_bsgs_batch(const JobDev &rep, const BatchItem *items, uint32_t nitems, uint32_t stage_max,
                               uint32_t warp_bytes, int grid, cudaStream_t st);
 
-cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
-                                 uint32_t total_words, uint32_t *bits, cudaStream_t st);
+// Build the character tables sel[0..nsel) of a job's list (odd parts kodd[],
+// word offsets word_off[] into bits); first[] are the running word counts of
+// the selected tables, total_words their sum.
+cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, const uint32_t *sel,
+                                 const uint32_t *first, uint32_t nsel, uint32_t total_words, uint32_t *bits,
+                                 cudaStream_t st);
 // Record an error for rs_last_error() and return code (rs_host.cu).
 int set_error(int code, const char *fmt, ...);
 

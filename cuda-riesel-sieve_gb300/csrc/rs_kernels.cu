@@ -492,31 +492,38 @@ __global__ void __launch_bounds__(128) setup_kernel(JobDev J, ChunkBufs cb) {
 }
 
 // Quadratic-character tables: word w of the table of odd k' holds bit t =
-// ((32*w + t) / k') == +1 (Jacobi symbol), for 32*w + t < k'.
-__global__ void jacobi_table_kernel(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
-                                    uint32_t total_words, uint32_t *bits) {
-  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= total_words) return;
-  uint32_t lo = 0, hi = ntab;  // last table with word_off <= w
+// ((32*w + t) / k') == +1 (Jacobi symbol), for 32*w + t < k'.  One launch
+// builds the tables sel[0..nsel) of the job's list (odd parts kodd[], word
+// offsets word_off[]); thread g writes word g - first[i] of table sel[i], where
+// first[] are the running word counts of the selected tables.
+__global__ void jacobi_table_kernel(const uint32_t *kodd, const uint32_t *word_off, const uint32_t *sel,
+                                    const uint32_t *first, uint32_t nsel, uint32_t total_words, uint32_t *bits) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_words) return;
+  uint32_t lo = 0, hi = nsel;  // last selected table with first <= g
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) / 2;
-    if (word_off[mid] <= w) lo = mid;
+    if (first[mid] <= g) lo = mid;
     else hi = mid;
   }
-  const uint32_t k = kodd[lo];
-  const uint32_t a0 = 32 * (w - word_off[lo]);
+  const uint32_t t = sel[lo];
+  const uint32_t k = kodd[t];
+  const uint32_t w = g - first[lo];
+  const uint32_t a0 = 32 * w;
   uint32_t out = 0;
-  for (uint32_t t = 0; t < 32; t++) {
-    const uint32_t a = a0 + t;
-    if (a < k && jacobi32(a, k) == 1) out |= 1u << t;
+  for (uint32_t b = 0; b < 32; b++) {
+    const uint32_t a = a0 + b;
+    if (a < k && jacobi32(a, k) == 1) out |= 1u << b;
   }
-  bits[w] = out;
+  bits[word_off[t] + w] = out;
 }
 
-cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, uint32_t ntab,
-                                 uint32_t total_words, uint32_t *bits, cudaStream_t st) {
-  if (total_words == 0) return cudaSuccess;
-  jacobi_table_kernel<<<(total_words + 255) / 256, 256, 0, st>>>(kodd, word_off, ntab, total_words, bits);
+cudaError_t launch_jacobi_tables(const uint32_t *kodd, const uint32_t *word_off, const uint32_t *sel,
+                                 const uint32_t *first, uint32_t nsel, uint32_t total_words, uint32_t *bits,
+                                 cudaStream_t st) {
+  if (total_words == 0 || nsel == 0) return cudaSuccess;
+  jacobi_table_kernel<<<(total_words + 255) / 256, 256, 0, st>>>(kodd, word_off, sel, first, nsel, total_words,
+                                                                 bits);
   return cudaGetLastError();
 }
 

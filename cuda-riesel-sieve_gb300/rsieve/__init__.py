@@ -26,6 +26,8 @@ RS_ERR_TIMEOUT = 9
 
 # rs_options.baby_step
 BABY_AUTO, BABY_SHOUP, BABY_SHORT, BABY_HIGH = 0, 1, 2, 3
+# rs_options.char_tables: when the per-k quadratic-character tables are built
+TABLES_AUTO, TABLES_ALWAYS, TABLES_NEVER = 0, 1, 2
 
 # rs_gpu_modmul_check operations
 OPS = {"montmul": 0, "from_mont": 1, "shoup_const": 2, "shoup": 3, "shoup32": 4, "shoup_w32": 5,
@@ -63,6 +65,7 @@ class Options(ctypes.Structure):
         ("host_verify", ctypes.c_int32),
         ("device", ctypes.c_int32),
         ("baby_step", ctypes.c_int32),
+        ("char_tables", ctypes.c_int32),
         ("mem_limit", ctypes.c_uint64),
     ]
 

@@ -52,6 +52,16 @@ typedef struct rs_job rs_job;
 #define RS_BABY_HIGH 3   /* Shoup's product by a 32-bit constant: b^Q * 2^32 < p, CTA-per-prime
                             layout only (the warp layout then takes RS_BABY_SHOUP) */
 
+/* rs_options.char_tables: the quadratic character (k/p) of every k is read
+ * from a bit table of (a/k') over a in [0, k'), k' the odd part of k, when the
+ * table exists, else computed (a Jacobi symbol per prime and k).  A table costs
+ * one Jacobi symbol per entry to build on the device, so it pays once the job
+ * has sieved more primes than k'. */
+#define RS_TABLES_AUTO 0    /* build each table when the primes the job has sieved, with
+                               those of the range about to be sieved, reach its k' */
+#define RS_TABLES_ALWAYS 1  /* build every table when the job is created */
+#define RS_TABLES_NEVER 2   /* no tables: compute every character */
+
 /* One removed candidate: p | k*b^n+c. */
 typedef struct {
   uint64_t p;
@@ -80,6 +90,8 @@ typedef struct {
                            picks, per launch, the cheapest form valid for every
                            prime of it; the others force a form where it is valid
                            (else AUTO) -- results are identical, only speed differs */
+  int32_t char_tables;  /* RS_TABLES_*: when the per-k character tables are built (no
+                           counterpart; results are identical, only speed differs) */
   uint64_t mem_limit;   /* device bytes for the job's per-launch buffers, which set the
                            primes per launch when -b/-t are not given; 0 = 3 GiB */
 } rs_options;

@@ -271,6 +271,40 @@ def test_wide_job_near_2_35(rs, oracle_mod, baby_step, datless):
     assert st["primes_by_step"][want] == st["primes"]
 
 
+@pytest.mark.parametrize("mode", ["auto", "always", "never"])
+def test_character_table_modes(rs, oracle_mod, mode):
+    """The quadratic characters from bit tables built when they pay (auto: here,
+    on a 2e5-wide window, only tables of k' below ~6,000), all at creation
+    (always) or none (never), on the wide b=2 job (1000 k up to 1e7) at 2^35,
+    both complete and datless: the same factor sets as the oracle."""
+    b, s, ks, nl = _wide_job()
+    m = {"auto": rs.TABLES_AUTO, "always": rs.TABLES_ALWAYS, "never": rs.TABLES_NEVER}[mode]
+    p0 = 2**35 + 1
+    for datless in (False, True):
+        g, o, st = _both(rs, oracle_mod, b, s, ks, nl, p0, p0 + 2 * 10**5 - 1, datless=datless, char_tables=m)
+        assert len(o) >= 5 and g == o
+
+
+def test_character_tables_built_as_primes_accumulate(rs, oracle_mod):
+    """One job (auto tables) over consecutive windows of growing width: each
+    call builds the tables its primes pay for, and every window's factors
+    equal the oracle's; sieving the first window again gives the same set."""
+    import rsieve.synth as S
+
+    (b, s, ks, nl), _ = S.batch_job(7, 20)  # a CTA-layout job of many k
+    oj = oracle_mod.Job.from_arrays(b, s, ks, [np.asarray(x) for x in nl])
+    p0 = 2**33 + 1
+    wins = [(p0, p0 + 2 * 10**5 - 1), (p0 + 2 * 10**5, p0 + 10**6 - 1), (p0 + 10**6, p0 + 6 * 10**6 - 1)]
+    with rs.Job(base=b, sign=s, ks=ks, nlists=nl, datless=1) as job:
+        first = None
+        for a, z in wins:
+            g, st = job.sieve(a, z)
+            o, npr = oj.sieve(a, z, datless=True)
+            assert st["primes"] == npr and _set(g) == _set(o)
+            first = first or _set(g)
+        assert _set(job.sieve(*wins[0])[0]) == first
+
+
 @pytest.mark.parametrize("i", [0, 1, 2, 3])
 def test_batch_shaped_jobs(rs, oracle_mod, i):
     """Jobs drawn from the mixed-batch distribution (random base, k count,
